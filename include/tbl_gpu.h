@@ -1,0 +1,187 @@
+/*
+ * tbl_gpu.h -- C ABI of the GB300 (sm_103a) time-step library for the
+ * spatially developing turbulent boundary layer DNS of theparvezahmad/turbulentBL.
+ *
+ * The library replaces the body of the reference's time loop
+ *     dnstbl2/dnstbl.f90:538-2375  (do while (nstep < maxstep) ... end do)
+ * i.e. the recycling inflow, convection + explicit RHS, Gauss-Seidel implicit
+ * diffusion, divergence, SSOR-preconditioned GMRES pressure-Poisson solve,
+ * projection, boundary conditions, per-step statistics and the every-`cum`
+ * recycling/rescaling bookkeeping.  The reference has no plugin or FFI API of
+ * its own: its state is the program-global arrays Ut, Press, PCorr, usum2,
+ * vsum2, wsum2, Wt, Ufluc, new, lamda and the mesh x1,x2,x3,Jac,Jac2.  Every
+ * entry point below names the reference lines whose state or work it takes
+ * over.
+ *
+ * Conventions (identical to the reference arrays):
+ *   - 3-D fields are Fortran column-major, i (streamwise) fastest, then j
+ *     (spanwise, periodic, j=1 and j=ny are ghost copies of ny-1 and 2), then
+ *     k (wall-normal, wall at k=1).  Size nx*ny*nz doubles.
+ *   - 2-D statistics arrays are (nx, nz), i fastest.
+ *   - Index arrays (new(k)) hold the reference's 1-based values.
+ *   - Host pointers are borrowed for the duration of a call only; the handle
+ *     owns all device memory.  One host thread per handle.
+ *   - Every function returns TBL_OK (0) or a negative TBL_ERR_* code; nothing
+ *     aborts or throws across the ABI.
+ */
+#ifndef TBL_GPU_H
+#define TBL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TBL_ABI_VERSION 1
+
+/* status codes */
+#define TBL_OK                 0
+#define TBL_ERR_CUDA          -1  /* a CUDA runtime call failed */
+#define TBL_ERR_BAD_ARG       -2  /* invalid configuration or pointer */
+#define TBL_ERR_NOT_CONVERGED -3  /* GS or GMRES hit mmax (reference continues silently) */
+#define TBL_ERR_NAN           -4  /* NaN/Inf found in the state after a step */
+#define TBL_ERR_BLOWUP        -5  /* u',v' or w' > 25 (reference STOP, dnstbl2/dnstbl.f90:1749-1775) */
+#define TBL_ERR_TIMEOUT       -6  /* a bounded device wait gave up */
+#define TBL_ERR_NO_DEVICE     -7  /* no CUDA device / library built without it */
+#define TBL_ERR_REPLAY        -8  /* replay counts exhausted or inconsistent */
+#define TBL_ERR_ZERO_RHS      -9  /* zero preconditioned PPE residual at restart 1 (reference divides by zero) */
+
+/* precision modes */
+#define TBL_PREC_FP64   0   /* the plain method: every field and operation in FP64 */
+#define TBL_PREC_MIXED  1   /* FP32 stencils/storage/inner GMRES inside FP64 iterative refinement */
+
+/* flags */
+#define TBL_FLAG_REPLAY        1  /* follow counts given by tbl_set_replay instead of testing convergence */
+#define TBL_FLAG_PPE_RESIDUAL  2  /* compute the true relative PPE residual after each solve */
+#define TBL_FLAG_DIAGNOSTICS   4  /* divergence / mass-flux / wall-shear / KE diagnostics every step */
+
+/* Run parameters.  The reference hard-codes all of them as literals
+ * (dnstbl2/dnstbl.f90:20-140); here they are one plain struct. */
+typedef struct tbl_config {
+    int32_t nx, ny, nz;     /* n3d(1..3); ny includes the 2 periodic ghost rows */
+    int32_t nproc;          /* virtual MPI ranks P (slab decomposition in k, :469-475) */
+    int32_t irec;           /* recycling plane, 1-based (reference: 68, :560) */
+    int32_t cum;            /* recycling / statistics window in steps (reference: 5, :115) */
+    int32_t istat;          /* statistics period (reference: 1, :28) */
+    int32_t recycle_after;  /* recycled inflow when nstep > this (reference: 5, :557) */
+    int32_t kmax;           /* GMRES restart length (reference: 50, :138) */
+    int32_t mmax;           /* max GS sweeps and max GMRES restarts (reference: 1000, :139) */
+    int32_t precision;      /* TBL_PREC_* */
+    int32_t flags;          /* TBL_FLAG_* */
+    int32_t mixed_kmax;     /* inner FP32 GMRES restart length (mixed mode) */
+    int32_t mixed_max_outer;/* max FP64 refinement sweeps (mixed mode) */
+    double dt;              /* time step (reference: 1e-4, :34) */
+    double re;              /* Reynolds number (reference: 150.92, :48) */
+    double ue;              /* free-stream velocity (reference: 19.798, :113) */
+    double dx, dy, dxi;     /* uniform spacings in x1, x2 and the computational xi (:401-403) */
+    double omega;           /* SSOR relaxation w (reference: REAL(4) 1.835, :140) */
+    double errtol;          /* GMRES relative tolerance (reference: 1e-5, :137) */
+    double errorstop;       /* GS L1 residual ratio (reference: 1e-6, :23) */
+    double mixed_inner_tol; /* inner FP32 GMRES relative tolerance (mixed mode) */
+    double mixed_outer_tol; /* FP64 refinement residual target, relative (mixed mode) */
+} tbl_config;
+
+/* Mesh, host-computed once (dnstbl2/dnstbl.f90:392-426): x1(nx), x2(ny),
+ * x3(nz), Jac(nz) = dx3/dxi and Jac2(nz) = d2x3/dxi2, NOT inverted. */
+typedef struct tbl_mesh {
+    const double* x1;
+    const double* x2;
+    const double* x3;
+    const double* jac;
+    const double* jac2;
+} tbl_mesh;
+
+/* The restart state (the 15 columns of 3D.tp, dnstbl2/dnstbl.f90:350-358,
+ * plus the scalars the program carries).  Used for upload and download; in
+ * download any pointer may be NULL to skip that array. */
+typedef struct tbl_state {
+    double* u; double* v; double* w;        /* Ut(:,:,:,1..3), nx*ny*nz */
+    double* p;                              /* Press */
+    double* pcorr;                          /* PCorr (GMRES warm start) */
+    double* usum2; double* vsum2; double* wsum2;  /* recycling means (nx,nz) */
+    double* wt;                             /* Wt(nx,nz) */
+    double* uf; double* vf; double* wf;     /* Ufluc(:,:,:,1..3), nx*ny*nz */
+    int32_t* newk;                          /* new(nz), 1-based */
+    double* ume1;                           /* Ume1(1,k): fixed inflow mean, nz */
+    double* bltkns;                         /* boundary-layer thickness bltkns(nx) */
+    double lamda;                           /* u_tau ratio (reset to 1 at start, :441) */
+    double time;
+    int32_t nstep;                          /* from the 3D.tp header */
+    int32_t cont;                           /* steps since program start (drives cum) */
+    int32_t ksep;                           /* last inner index of the previous rescaling */
+    int32_t pad_;
+} tbl_state;
+
+/* Per-step report (replaces the reference's stdout/ASCII monitors). */
+typedef struct tbl_step_stats {
+    int32_t nstep;
+    int32_t status;
+    int32_t gs_sweeps[3];       /* GS sweeps per velocity component */
+    int32_t gmres_restarts;     /* GMRES outer restarts m */
+    int32_t gmres_iters;        /* total Arnoldi steps over all restarts */
+    int32_t cum_step;           /* 1 when the rescaling bookkeeping ran */
+    int32_t outer_iters;        /* mixed mode: FP64 refinement sweeps */
+    int32_t pad_;
+    double gs_resid[3];         /* final GS L1 ratio sumav */
+    double gmres_resid;         /* final GMRES estimate |g(kit+1)|/rho_0 */
+    double ppe_rel_resid;       /* ||L7 p' - Q8||_2 / ||Q8||_2 (flag TBL_FLAG_PPE_RESIDUAL) */
+    double div_diag;            /* |sum div| / N, the reference's printout (:1571-1577) */
+    double ke;                  /* kinetic energy of fluctuations (:1724-1741) */
+    double lamda;               /* current lamda */
+    double time;
+} tbl_step_stats;
+
+/* Statistics and rescaling outputs (dnstbl2/dnstbl.f90:1902-2277). */
+typedef struct tbl_stats_out {
+    double* usum; double* vsum; double* wsum;          /* running sums (nx,nz) */
+    double* uusum; double* vvsum; double* wwsum;
+    double* uvsum; double* uwsum; double* vwsum;
+    double* deltastar; double* theta; double* ht; double* reth;  /* (nx), last rescaling */
+    double* tauw_sum;                                  /* sumxz(nx) wall-shear accumulator */
+    double* ubulk;                                     /* mass flux at 5 planes (5) */
+    double lamda03;
+    int32_t nstat;
+    int32_t pad_;
+} tbl_stats_out;
+
+typedef struct tbl_handle tbl_handle;
+
+/* Create a handle on the current CUDA device; allocates all device memory,
+ * computes the stencil coefficients (dnstbl2/dnstbl.f90:487-536). */
+int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out);
+
+/* Upload the restart state (replaces the 3D.tp read, :350-358). */
+int tbl_upload_state(tbl_handle* h, const tbl_state* st);
+
+/* Advance nsteps time steps (the loop body :538-2375).  stats may be NULL,
+ * else it receives nsteps records. */
+int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats);
+
+/* Download the state (replaces the 3D%03d.tp write, :2380-2397). */
+int tbl_download_state(tbl_handle* h, tbl_state* st);
+
+/* Download the statistics accumulators and rescaling outputs. */
+int tbl_download_stats(tbl_handle* h, tbl_stats_out* out);
+
+/* Replay iteration counts (parity runs).  rec is a sequence of per-step
+ * records {gs1, gs2, gs3, nrestarts, kit_1 .. kit_nrestarts}; used when
+ * TBL_FLAG_REPLAY is set.  The library copies the array. */
+int tbl_set_replay(tbl_handle* h, const int32_t* rec, int64_t len);
+
+/* Iteration-count record of the most recent step in the replay format.
+ * Returns the record length (>= 4) or a negative status; writes at most cap. */
+int tbl_last_counts(tbl_handle* h, int32_t* buf, int32_t cap);
+
+/* Release everything. */
+void tbl_destroy(tbl_handle* h);
+
+const char* tbl_status_string(int status);
+
+/* Number of kernel launches issued by this handle so far (instrumentation). */
+int64_t tbl_launch_count(tbl_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TBL_GPU_H */

@@ -1,0 +1,35 @@
+"""ctypes binding of the C++ oracle (test infrastructure only)."""
+import ctypes as C
+
+import numpy as np
+
+from turbulentbl_gb300.runner import AbiRunner
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(_build.build())
+        _lib.orc_apply_lap.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.orc_apply_ssor.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    return _lib
+
+
+class OracleRunner(AbiRunner):
+    def __init__(self, mesh, rp):
+        super().__init__(lib(), "orc_", mesh, rp)
+
+    def apply_lap(self, x):
+        x = np.asfortranarray(x, dtype=np.float64)
+        y = np.zeros_like(x, order="F")
+        lib().orc_apply_lap(self._h, x.ctypes.data_as(C.POINTER(C.c_double)), y.ctypes.data_as(C.POINTER(C.c_double)))
+        return y
+
+    def apply_ssor(self, x):
+        x = np.asfortranarray(x, dtype=np.float64)
+        y = np.zeros_like(x, order="F")
+        lib().orc_apply_ssor(self._h, x.ctypes.data_as(C.POINTER(C.c_double)), y.ctypes.data_as(C.POINTER(C.c_double)))
+        return y

@@ -1,0 +1,531 @@
+// tbl_api.cu -- the C ABI (include/tbl_gpu.h): handle lifecycle, state
+// transfer and the per-step driver that sequences the kernels in the order
+// of the reference time loop (dnstbl2/dnstbl.f90:538-2375).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "tbl_internal.cuh"
+#include "tbl_kernels.cuh"
+
+namespace tbl {
+
+static thread_local char g_last_error[512] = {0};
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+}
+
+static int readback(tbl_handle* h, const void* dev, size_t bytes) {
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->hpin, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return TBL_OK;
+}
+
+// 3-D host (nx,ny,nz) <-> device (sx,ny,nz)
+static int put3(tbl_handle* h, double* dst, const double* src) {
+    const Geom& g = h->g;
+    TBL_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)g.sx * 8, src, (size_t)g.nx * 8, (size_t)g.nx * 8,
+                                   (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    return TBL_OK;
+}
+static int get3(tbl_handle* h, double* dst, const double* src) {
+    const Geom& g = h->g;
+    TBL_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)g.nx * 8, src, (size_t)g.sx * 8, (size_t)g.nx * 8,
+                                   (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, h->stream));
+    return TBL_OK;
+}
+
+template <typename T>
+static int dalloc(T** p, size_t n) {
+    TBL_CUDA_TRY(cudaMalloc((void**)p, n * sizeof(T)));
+    TBL_CUDA_TRY(cudaMemset(*p, 0, n * sizeof(T)));
+    return TBL_OK;
+}
+
+#define TRY(x)                          \
+    do {                                \
+        int s_ = (x);                   \
+        if (s_ != TBL_OK) return s_;    \
+    } while (0)
+
+static void free_all(tbl_handle* h) {
+    void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
+                    h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->usum2, h->vsum2,
+                    h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
+                    h->usum2_fl, h->sums, h->bl_out, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
+                    h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->hpin) cudaFreeHost(h->hpin);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* h) {
+    h->cfg = *cfg;
+    const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
+    Geom& g = h->g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.sx = ((nx + 2) + 7) / 8 * 8;
+    g.ps = (long long)g.sx * ny;
+    g.vol = g.ps * nz;
+    g.J = ny - 2;
+    h->P = cfg->nproc;
+    const int loc_n = (nz - 1) / h->P;  // (:469-475), 1-based bn = 2 + r*loc_n
+    h->bn.resize(h->P);
+    h->en.resize(h->P);
+    for (int r = 0; r < h->P; ++r) {
+        h->bn[r] = 1 + r * loc_n;
+        h->en[r] = h->bn[r] + loc_n - 1;
+        if (r == h->P - 1) h->en[r] = nz - 2;
+    }
+    TBL_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    TBL_CUDA_TRY(cudaMallocHost(&h->hpin, 4096));
+    const size_t vol = (size_t)g.vol, n2 = (size_t)nx * nz, pl = (size_t)ny * nz;
+    for (int c = 0; c < 3; ++c) { TRY(dalloc(&h->U[c], vol)); TRY(dalloc(&h->Q[c], vol)); }
+    TRY(dalloc(&h->Pr, vol)); TRY(dalloc(&h->PC, vol)); TRY(dalloc(&h->Q8, vol)); TRY(dalloc(&h->RH, vol));
+    TRY(dalloc(&h->V, vol * (size_t)(cfg->kmax + 1)));
+    TRY(dalloc(&h->uold1, pl));
+    TRY(dalloc(&h->x3, (size_t)nz)); TRY(dalloc(&h->jacinv, (size_t)nz)); TRY(dalloc(&h->jac2, (size_t)nz));
+    TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
+    TRY(dalloc(&h->rAp, (size_t)nz));
+    TRY(dalloc(&h->usum2, n2)); TRY(dalloc(&h->vsum2, n2)); TRY(dalloc(&h->wsum2, n2)); TRY(dalloc(&h->wt, n2));
+    TRY(dalloc(&h->ume1, (size_t)nz)); TRY(dalloc(&h->bltkns, (size_t)nx)); TRY(dalloc(&h->newk, (size_t)nz));
+    TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));
+    TRY(dalloc(&h->ufl_full, 3 * vol)); TRY(dalloc(&h->usum2_fl, 3 * n2));
+    TRY(dalloc(&h->sums, 9 * n2)); TRY(dalloc(&h->bl_out, 4 * (size_t)nx));
+    TRY(dalloc(&h->slab_of_k, (size_t)nz));
+    TRY(dalloc(&h->sc, 1));
+    const int K1 = cfg->kmax + 1;
+    TRY(dalloc(&h->h, (size_t)K1 * K1)); TRY(dalloc(&h->gg, (size_t)K1)); TRY(dalloc(&h->gc, (size_t)K1));
+    TRY(dalloc(&h->gs, (size_t)K1)); TRY(dalloc(&h->gy, (size_t)K1));
+    h->red.max_blocks = 2048;
+    TRY(dalloc(&h->red.partial, (size_t)16 * h->red.max_blocks));
+    TRY(dalloc(&h->red.count, (size_t)16));
+    TRY(dalloc(&h->halo, (size_t)2 * 3 * 2 * h->P * g.ps));
+    TRY(dalloc(&h->err, 1));
+    // mesh and per-k coefficients (:487-536); An* == Av*
+    std::vector<double> x3(mesh->x3, mesh->x3 + nz), jinv(nz), j2(mesh->jac2, mesh->jac2 + nz);
+    std::vector<double> Ab(nz, 0.0), At(nz, 0.0), Ap(nz, 0.0), rAp(nz, 0.0);
+    const double dx = cfg->dx, dy = cfg->dy, dxi = cfg->dxi;
+    for (int k = 1; k <= nz - 2; ++k) {
+        double J = mesh->jac[k], J2 = mesh->jac2[k];
+        double a = 1.0 / (dxi * dxi * J * J);
+        double b = J2 / (2.0 * dxi * J * J * J);
+        Ab[k] = a + b;
+        At[k] = a - b;
+        Ap[k] = -2.0 * ((1.0 / (dx * dx)) + (1.0 / (dy * dy)) + (1.0 / (dxi * dxi * J * J)));
+        rAp[k] = 1.0 / Ap[k];
+    }
+    for (int k = 0; k < nz; ++k) jinv[k] = 1.0 / mesh->jac[k];
+    h->x3h = x3;
+    h->stats_A = mesh->x2[ny - 1] - mesh->x2[1];
+    TBL_CUDA_TRY(cudaMemcpy(h->x3, x3.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->jacinv, jinv.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->jac2, j2.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->Ab, Ab.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->At, At.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->Ap, Ap.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->rAp, rAp.data(), nz * 8, cudaMemcpyHostToDevice));
+    std::vector<int> sok(nz, 0);
+    for (int r = 0; r < h->P; ++r)
+        for (int k = h->bn[r]; k <= h->en[r]; ++k) sok[k] = r;
+    TBL_CUDA_TRY(cudaMemcpy(h->slab_of_k, sok.data(), nz * 4, cudaMemcpyHostToDevice));
+    DevScalars s0;
+    memset(&s0, 0, sizeof(s0));
+    s0.lamda = 1.0;
+    TBL_CUDA_TRY(cudaMemcpy(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice));
+    TRY(build_sweep_ctas(h));
+    TRY(check_cooperative(h));
+    h->nstep = 0; h->cont = 0; h->nstat = 0; h->time = 0.0;
+    h->fluc_updated = false;
+    h->replay_pos = 0;
+    h->lamda_host = 1.0;
+    return TBL_OK;
+}
+
+// ------------------------------------------------------------ GS solve
+static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
+    const int mmax = h->cfg.mmax;
+    bool active[3] = {true, true, true};
+    int sweeps[3] = {0, 0, 0};
+    double sumnor[3] = {0, 0, 0}, sumav[3] = {0, 0, 0};
+    int parity = 0;
+    TRY(launch_halo_init(h, parity));
+    const int nb = red_blocks(h);
+    for (int it = 1; it <= mmax; ++it) {
+        int comps[3], n = 0;
+        for (int c = 0; c < 3; ++c)
+            if (active[c]) comps[n++] = c;
+        if (it % 2 == 1) {  // residual check every other sweep (:781-828)
+            TRY(launch_gs_resid(h, comps, n, nb > 512 ? 512 : nb));
+            TRY(readback(h, &h->sc->red[0], 3 * sizeof(double)));
+            const double* red = h->hpin;
+            int m = 0;
+            for (int q = 0; q < n; ++q) {
+                int c = comps[q];
+                double diver = red[c];
+                if (it == 1) sumnor[c] = 1.0 / diver;
+                sumav[c] = diver * sumnor[c];
+                bool stop = target ? (sweeps[c] >= target[c]) : (sumav[c] < h->cfg.errorstop);
+                if (stop) active[c] = false;
+                else comps[m++] = c;
+            }
+            n = m;
+            if (n == 0) break;
+        }
+        TRY(launch_gs_sweep(h, comps, n, parity));
+        parity ^= 1;
+        for (int q = 0; q < n; ++q) sweeps[comps[q]]++;
+    }
+    for (int c = 0; c < 3; ++c) { st.gs_sweeps[c] = sweeps[c]; st.gs_resid[c] = sumav[c]; }
+    return TBL_OK;
+}
+
+// ------------------------------------------------------------ GMRES
+static int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_step_stats& st) {
+    const int kmax = h->cfg.kmax, K1 = kmax + 1;
+    const size_t vol = (size_t)h->g.vol;
+    double sumav = 1.0;
+    int m = 0, iters = 0;
+    const int nr = rec ? rec[0] : 0;
+    int status = TBL_OK;
+    while (rec ? (m < nr) : ((sumav > h->cfg.errtol) && (m < h->cfg.mmax))) {
+        m = m + 1;
+        double* V0 = h->V;
+        TRY(launch_ssor_fwd(h, h->PC, h->Q8));  // r = Q8 - L7 p', then SSOR (:995-1042)
+        TRY(launch_ssor_bwd(h, V0));
+        TRY(launch_dot(h, V0, V0, &h->sc->rho, 1));
+        TRY(launch_restart_init(h, m == 1));
+        TRY(readback(h, &h->sc->rho, 4 * sizeof(double)));  // rho, sumnor, sumav
+        double rho = h->hpin[0];
+        if (m == 1 && !(rho > 0.0)) { status = TBL_ERR_ZERO_RHS; break; }
+        sumav = h->hpin[2];
+        TRY(launch_scale_by_inv(h, V0, &h->sc->rho));
+        int kit = 0;
+        const int target = rec ? rec[m] : 0;
+        while (rec ? (kit < target) : ((sumav > h->cfg.errtol) && (kit < kmax))) {
+            kit = kit + 1;
+            double* W = h->V + (size_t)kit * vol;
+            TRY(launch_ssor_fwd(h, h->V + (size_t)(kit - 1) * vol, nullptr));
+            TRY(launch_ssor_bwd(h, W));
+            double* hcol = h->h + (size_t)K1 * (kit - 1);
+            TRY(launch_mgs(h, W, nullptr, nullptr, V0, &hcol[0], 0));
+            for (int kk = 1; kk <= kit - 1; ++kk)
+                TRY(launch_mgs(h, W, h->V + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->V + (size_t)kk * vol, &hcol[kk], 0));
+            TRY(launch_mgs(h, W, h->V + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
+            TRY(launch_givens(h, kit));
+            TRY(launch_scale_by_inv(h, W, &h->sc->red[8]));
+            TRY(readback(h, &h->sc->sumav, sizeof(double)));
+            sumav = h->hpin[0];
+        }
+        iters += kit;
+        kits.push_back(kit);
+        if (kit > 0) TRY(launch_backsub_update(h, kit));
+    }
+    st.gmres_restarts = m;
+    st.gmres_iters = iters;
+    st.gmres_resid = sumav;
+    if (status == TBL_OK && !rec && sumav > h->cfg.errtol) status = TBL_ERR_NOT_CONVERGED;
+    return status;
+}
+
+static int one_step(tbl_handle* h, tbl_step_stats* out) {
+    tbl_step_stats st;
+    memset(&st, 0, sizeof(st));
+    const tbl_config& c = h->cfg;
+    h->time = h->time + c.dt;
+    h->nstep = h->nstep + 1;
+    // replay record for this step
+    const bool replay = (c.flags & TBL_FLAG_REPLAY) != 0;
+    const int32_t* rec = nullptr;
+    int gs_target[3];
+    if (replay) {
+        if (h->replay_pos + 4 > h->replay.size()) return TBL_ERR_REPLAY;
+        const int32_t* r = h->replay.data() + h->replay_pos;
+        for (int q = 0; q < 3; ++q) gs_target[q] = r[q];
+        if (h->replay_pos + 4 + (size_t)r[3] > h->replay.size()) return TBL_ERR_REPLAY;
+        rec = r + 3;
+        h->replay_pos += 4 + r[3];
+    }
+    TRY(launch_save_uold(h));
+    if (h->nstep > c.recycle_after) TRY(launch_inflow(h));
+    TRY(launch_conv_q(h));
+    TRY(gs_solve(h, replay ? gs_target : nullptr, st));
+    TRY(launch_div(h));
+    TRY(launch_pc_zero_faces(h));
+    std::vector<int32_t> kits;
+    int status = gmres(h, rec, kits, st);
+    if (status == TBL_ERR_ZERO_RHS || status < 0 && status != TBL_ERR_NOT_CONVERGED) return status;
+    if (c.flags & TBL_FLAG_PPE_RESIDUAL) {
+        TRY(launch_ppe_resid(h));
+        TRY(readback(h, &h->sc->red[9], 2 * sizeof(double)));
+        st.ppe_rel_resid = h->hpin[1] > 0 ? std::sqrt(h->hpin[0] / h->hpin[1]) : 0.0;
+    }
+    TRY(launch_project_bcs(h));
+    const int nb = red_blocks(h);
+    TRY(launch_div_diag(h, nb > 512 ? 512 : nb, 3));
+    const bool fluc = h->nstep > c.recycle_after;
+    if (fluc) {
+        TRY(launch_fluc_ke(h, nb > 512 ? 512 : nb, 4));
+        const size_t n2 = (size_t)c.nx * c.nz;
+        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl, h->usum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + n2, h->vsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + 2 * n2, h->wsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+        h->fluc_updated = true;
+    }
+    h->cont = h->cont + 1;
+    if (h->nstep % c.istat == 0) {
+        TRY(launch_stats(h));
+        h->nstat++;
+    }
+    st.cum_step = 0;
+    if (h->cont % c.cum == 0) {
+        TRY(launch_rescale(h));
+        st.cum_step = 1;
+    }
+    // scalars back: red[3] div, red[4] KE, red[5] max fluct, lamda, err
+    TRY(readback(h, h->sc, sizeof(DevScalars)));
+    DevScalars sc;
+    memcpy(&sc, h->hpin, sizeof(sc));
+    int err = 0;
+    TBL_CUDA_TRY(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+    st.div_diag = std::fabs(sc.red[3]) / ((double)(c.ny - 2) * (c.nx - 2) * (c.nz - 2));
+    st.ke = fluc ? sc.red[4] / ((double)c.nx * (c.ny - 2) * (c.nz - 2)) : 0.0;
+    st.lamda = sc.lamda;
+    h->lamda_host = sc.lamda;
+    st.nstep = h->nstep;
+    st.time = h->time;
+    h->last_counts.clear();
+    for (int q = 0; q < 3; ++q) h->last_counts.push_back(st.gs_sweeps[q]);
+    h->last_counts.push_back((int32_t)kits.size());
+    for (int q : kits) h->last_counts.push_back(q);
+    if (err != 0) status = err;
+    else if (!std::isfinite(sc.red[3]) || (fluc && !std::isfinite(sc.red[4]))) status = TBL_ERR_NAN;
+    else if (fluc && sc.red[5] > 25.0) status = TBL_ERR_BLOWUP;
+    else if (status == TBL_OK && !replay)
+        for (int q = 0; q < 3; ++q)
+            if (st.gs_sweeps[q] >= c.mmax) status = TBL_ERR_NOT_CONVERGED;
+    st.status = status;
+    if (out) *out = st;
+    return status;
+}
+
+}  // namespace tbl
+
+using namespace tbl;
+
+extern "C" {
+
+int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
+    if (!cfg || !mesh || !out || !mesh->x1 || !mesh->x2 || !mesh->x3 || !mesh->jac || !mesh->jac2)
+        return TBL_ERR_BAD_ARG;
+    if (cfg->nx < 8 || cfg->ny < 6 || cfg->nz < 8 || cfg->nproc < 1) return TBL_ERR_BAD_ARG;
+    if ((cfg->nz - 1) / cfg->nproc < 3) return TBL_ERR_BAD_ARG;
+    if (cfg->irec < 2 || cfg->irec > cfg->nx - 1 || cfg->cum < 1 || cfg->istat < 1) return TBL_ERR_BAD_ARG;
+    if (cfg->kmax < 1 || cfg->mmax < 1 || !(cfg->dt > 0) || !(cfg->re > 0)) return TBL_ERR_BAD_ARG;
+    if (cfg->precision != TBL_PREC_FP64 && cfg->precision != TBL_PREC_MIXED) return TBL_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TBL_ERR_NO_DEVICE;
+    tbl_handle* h = new (std::nothrow) tbl_handle();
+    if (!h) return TBL_ERR_BAD_ARG;
+    memset((void*)&h->cfg, 0, sizeof(h->cfg));
+    h->U[0] = h->U[1] = h->U[2] = nullptr;
+    int s = create_impl(cfg, mesh, h);
+    if (s != TBL_OK) {
+        free_all(h);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return TBL_OK;
+}
+
+int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
+    if (!h || !st || !st->u || !st->v || !st->w || !st->p || !st->usum2 || !st->vsum2 || !st->wsum2 || !st->wt ||
+        !st->newk || !st->ume1)
+        return TBL_ERR_BAD_ARG;
+    const tbl_config& c = h->cfg;
+    for (int k = 0; k < c.nz; ++k)
+        if (st->newk[k] < 1 || st->newk[k] > c.nz) return TBL_ERR_BAD_ARG;
+    const size_t n2 = (size_t)c.nx * c.nz, pl = (size_t)c.ny * c.nz;
+    TRY(put3(h, h->U[0], st->u));
+    TRY(put3(h, h->U[1], st->v));
+    TRY(put3(h, h->U[2], st->w));
+    TRY(put3(h, h->Pr, st->p));
+    if (st->pcorr) TRY(put3(h, h->PC, st->pcorr));
+    else TBL_CUDA_TRY(cudaMemsetAsync(h->PC, 0, (size_t)h->g.vol * 8, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2, st->usum2, n2 * 8, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->vsum2, st->vsum2, n2 * 8, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->wsum2, st->wsum2, n2 * 8, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->wt, st->wt, n2 * 8, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->newk, st->newk, (size_t)c.nz * 4, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->ume1, st->ume1, (size_t)c.nz * 8, cudaMemcpyHostToDevice, h->stream));
+    if (st->bltkns)
+        TBL_CUDA_TRY(cudaMemcpyAsync(h->bltkns, st->bltkns, (size_t)c.nx * 8, cudaMemcpyHostToDevice, h->stream));
+    // Ufluc: full copy for the restart output and the recycling plane (file and live copies)
+    std::vector<double> plane(3 * pl, 0.0);
+    const double* uf[3] = {st->uf, st->vf, st->wf};
+    const double* us[3] = {st->usum2, st->vsum2, st->wsum2};
+    const double* U[3] = {st->u, st->v, st->w};
+    const int ir = c.irec - 1;
+    for (int cc = 0; cc < 3; ++cc) {
+        for (int k = 0; k < c.nz; ++k)
+            for (int j = 0; j < c.ny; ++j) {
+                size_t p = (size_t)ir + (size_t)c.nx * ((size_t)j + (size_t)c.ny * k);
+                plane[cc * pl + (size_t)j + (size_t)c.ny * k] =
+                    uf[cc] ? uf[cc][p] : (U[cc][p] - us[cc][(size_t)ir + (size_t)c.nx * k]);
+            }
+        if (uf[cc]) TRY(put3(h, h->ufl_full + (size_t)cc * h->g.vol, uf[cc]));
+        else TBL_CUDA_TRY(cudaMemsetAsync(h->ufl_full + (size_t)cc * h->g.vol, 0, (size_t)h->g.vol * 8, h->stream));
+    }
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->ufl_file, plane.data(), 3 * pl * 8, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->ufl_live, plane.data(), 3 * pl * 8, cudaMemcpyHostToDevice, h->stream));
+    // scalars
+    DevScalars s0;
+    TBL_CUDA_TRY(cudaMemcpyAsync(&s0, h->sc, sizeof(s0), cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    s0.lamda = st->lamda;
+    s0.ksep = st->ksep;
+    TBL_CUDA_TRY(cudaMemcpy(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemsetAsync(h->sums, 0, 9 * n2 * 8, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->nstep = st->nstep;
+    h->cont = st->cont;
+    h->time = st->time;
+    h->fluc_updated = false;
+    h->lamda_host = st->lamda;
+    return TBL_OK;
+}
+
+int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
+    if (!h || nsteps < 0) return TBL_ERR_BAD_ARG;
+    int last = TBL_OK;
+    for (int s = 0; s < nsteps; ++s) {
+        last = one_step(h, stats ? &stats[s] : nullptr);
+        if (last == TBL_ERR_NAN || last == TBL_ERR_BLOWUP || last == TBL_ERR_REPLAY || last == TBL_ERR_ZERO_RHS ||
+            last == TBL_ERR_CUDA || last == TBL_ERR_TIMEOUT)
+            return last;
+    }
+    return last;
+}
+
+int tbl_download_state(tbl_handle* h, tbl_state* st) {
+    if (!h || !st) return TBL_ERR_BAD_ARG;
+    const tbl_config& c = h->cfg;
+    const size_t n2 = (size_t)c.nx * c.nz, pl = (size_t)c.ny * c.nz, N = (size_t)c.nx * c.ny * c.nz;
+    if (st->u) TRY(get3(h, st->u, h->U[0]));
+    if (st->v) TRY(get3(h, st->v, h->U[1]));
+    if (st->w) TRY(get3(h, st->w, h->U[2]));
+    if (st->p) TRY(get3(h, st->p, h->Pr));
+    if (st->pcorr) TRY(get3(h, st->pcorr, h->PC));
+    if (st->usum2) TBL_CUDA_TRY(cudaMemcpyAsync(st->usum2, h->usum2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (st->vsum2) TBL_CUDA_TRY(cudaMemcpyAsync(st->vsum2, h->vsum2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (st->wsum2) TBL_CUDA_TRY(cudaMemcpyAsync(st->wsum2, h->wsum2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (st->wt) TBL_CUDA_TRY(cudaMemcpyAsync(st->wt, h->wt, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (st->newk) TBL_CUDA_TRY(cudaMemcpyAsync(st->newk, h->newk, (size_t)c.nz * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (st->ume1) TBL_CUDA_TRY(cudaMemcpyAsync(st->ume1, h->ume1, (size_t)c.nz * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (st->bltkns)
+        TBL_CUDA_TRY(cudaMemcpyAsync(st->bltkns, h->bltkns, (size_t)c.nx * 8, cudaMemcpyDeviceToHost, h->stream));
+    double* uf[3] = {st->uf, st->vf, st->wf};
+    bool any_uf = uf[0] || uf[1] || uf[2];
+    if (any_uf) {
+        // Ufluc as the reference holds it: uploaded columns, overwritten on the
+        // slabs' planes by the last per-step update U - means (:1712-1722), and
+        // the recycling plane by its live copy (:2341-2349).
+        std::vector<double> U(N), live(3 * pl), means(3 * n2);
+        TBL_CUDA_TRY(cudaMemcpyAsync(live.data(), h->ufl_live, 3 * pl * 8, cudaMemcpyDeviceToHost, h->stream));
+        TBL_CUDA_TRY(cudaMemcpyAsync(means.data(), h->usum2_fl, 3 * n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+        for (int cc = 0; cc < 3; ++cc) {
+            if (!uf[cc]) continue;
+            TRY(get3(h, uf[cc], h->ufl_full + (size_t)cc * h->g.vol));
+            TRY(get3(h, U.data(), h->U[cc]));
+            TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+            if (h->fluc_updated)
+                for (int k = 1; k <= c.nz - 2; ++k)
+                    for (int j = 1; j <= c.ny - 2; ++j)
+                        for (int i = 0; i < c.nx; ++i) {
+                            size_t p = (size_t)i + (size_t)c.nx * ((size_t)j + (size_t)c.ny * k);
+                            uf[cc][p] = U[p] - means[cc * n2 + (size_t)i + (size_t)c.nx * k];
+                        }
+            const int ir = c.irec - 1;
+            for (int k = 1; k <= c.nz - 2; ++k)
+                for (int j = 1; j <= c.ny - 2; ++j)
+                    uf[cc][(size_t)ir + (size_t)c.nx * ((size_t)j + (size_t)c.ny * k)] =
+                        live[cc * pl + (size_t)j + (size_t)c.ny * k];
+        }
+    }
+    DevScalars sc;
+    TBL_CUDA_TRY(cudaMemcpyAsync(&sc, h->sc, sizeof(sc), cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    st->lamda = sc.lamda;
+    st->ksep = sc.ksep;
+    st->time = h->time;
+    st->nstep = h->nstep;
+    st->cont = h->cont;
+    return TBL_OK;
+}
+
+int tbl_download_stats(tbl_handle* h, tbl_stats_out* out) {
+    if (!h || !out) return TBL_ERR_BAD_ARG;
+    const tbl_config& c = h->cfg;
+    const size_t n2 = (size_t)c.nx * c.nz;
+    double* dst[9] = {out->usum, out->vsum, out->wsum, out->uusum, out->vvsum, out->wwsum, out->uvsum, out->uwsum, out->vwsum};
+    for (int q = 0; q < 9; ++q)
+        if (dst[q]) TBL_CUDA_TRY(cudaMemcpyAsync(dst[q], h->sums + q * n2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    double* bl[4] = {out->deltastar, out->theta, out->ht, out->reth};
+    for (int q = 0; q < 4; ++q)
+        if (bl[q]) TBL_CUDA_TRY(cudaMemcpyAsync(bl[q], h->bl_out + (size_t)q * c.nx, (size_t)c.nx * 8,
+                                                cudaMemcpyDeviceToHost, h->stream));
+    DevScalars sc;
+    TBL_CUDA_TRY(cudaMemcpyAsync(&sc, h->sc, sizeof(sc), cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (out->tauw_sum) memset(out->tauw_sum, 0, (size_t)c.nx * 8);
+    if (out->ubulk) memset(out->ubulk, 0, 5 * 8);
+    out->lamda03 = sc.lamda03;
+    out->nstat = h->nstat;
+    return TBL_OK;
+}
+
+int tbl_set_replay(tbl_handle* h, const int32_t* rec, int64_t len) {
+    if (!h || len < 0 || (len > 0 && !rec)) return TBL_ERR_BAD_ARG;
+    h->replay.assign(rec, rec + len);
+    h->replay_pos = 0;
+    return TBL_OK;
+}
+
+int tbl_last_counts(tbl_handle* h, int32_t* buf, int32_t cap) {
+    if (!h || (cap > 0 && !buf)) return TBL_ERR_BAD_ARG;
+    int n = (int)h->last_counts.size();
+    for (int q = 0; q < n && q < cap; ++q) buf[q] = h->last_counts[q];
+    return n;
+}
+
+void tbl_destroy(tbl_handle* h) {
+    if (!h) return;
+    cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+}
+
+const char* tbl_status_string(int status) {
+    switch (status) {
+        case TBL_OK: return "ok";
+        case TBL_ERR_CUDA: return g_last_error[0] ? g_last_error : "CUDA runtime error";
+        case TBL_ERR_BAD_ARG: return "invalid argument";
+        case TBL_ERR_NOT_CONVERGED: return "GS or GMRES reached mmax";
+        case TBL_ERR_NAN: return "non-finite value in the state";
+        case TBL_ERR_BLOWUP: return "fluctuation above 25 (reference blow-up stop)";
+        case TBL_ERR_TIMEOUT: return "bounded device wait gave up";
+        case TBL_ERR_NO_DEVICE: return "no CUDA device";
+        case TBL_ERR_REPLAY: return "replay counts exhausted";
+        case TBL_ERR_ZERO_RHS: return "zero PPE residual at the first restart";
+        default: return "unknown status";
+    }
+}
+
+int64_t tbl_launch_count(tbl_handle* h) { return h ? h->launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// tbl_internal.cuh -- device state and kernel interfaces of libtblgpu.so.
+//
+// Layout in HBM: every 3-D field is the reference array Ut(nx,ny,nz,.) with
+// i fastest, stored with a row pitch sx = nx rounded up to 8 elements so that
+// each row starts on a 64-byte boundary (32-byte FP64 chunks stay aligned).
+// Element (i,j,k) (0-based) is at i + sx*(j + ny*k).  Padding columns hold 0.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <vector>
+
+#include "../../include/tbl_gpu.h"
+
+#define TBL_CUDA_TRY(expr)                                                    \
+    do {                                                                      \
+        cudaError_t e_ = (expr);                                              \
+        if (e_ != cudaSuccess) {                                              \
+            tbl::set_last_cuda_error(e_, #expr, __FILE__, __LINE__);          \
+            return TBL_ERR_CUDA;                                              \
+        }                                                                     \
+    } while (0)
+
+namespace tbl {
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+constexpr int CHUNK = 4;          // i-points per lane per wavefront step
+constexpr int KG = 4;             // k-planes (warps) per wavefront CTA
+constexpr int RED_THREADS = 256;  // threads per reduction block
+
+// Geometry shared by all kernels (passed by value).
+struct Geom {
+    int nx, ny, nz;   // reference n3d
+    int sx;           // row pitch
+    long long ps;     // plane stride sx*ny
+    long long vol;    // sx*ny*nz
+    int J;            // ny-2 unique spanwise rows
+};
+
+// One wavefront CTA: a 32-row x KG-plane block of (j,k) lines of one slab.
+struct SweepCta {
+    int slab;      // slab index r
+    int jb, kg;    // block coordinates inside the slab
+    int up_j;      // CTA index of (jb-1, kg) or -1
+    int up_k;      // CTA index of (jb, kg-1) or -1
+};
+
+// Slab s covers interior planes k in [bn, bn+K) (0-based).
+struct SlabDesc {
+    int bn, K;
+};
+
+// Device-side scalars of the recycling bookkeeping and of GMRES.
+struct DevScalars {
+    double lamda;
+    double lamda03;
+    int ksep;
+    int pad;
+    // GMRES
+    double rho, sumnor, sumav;
+    // reductions (result slots)
+    double red[16];
+};
+
+// Reduction workspace: partial sums + arrival counters per slot.
+struct RedWork {
+    double* partial;      // [slots][max_blocks]
+    unsigned int* count;  // [slots]
+    int max_blocks;
+};
+
+template <typename T>
+struct Fields {
+    T* U[3];
+    T* P;
+    T* PC;
+    T* Q[3];
+    T* Q8;
+};
+
+}  // namespace tbl
+
+struct tbl_handle {
+    tbl_config cfg;
+    tbl::Geom g;
+    int P;
+    std::vector<int> bn, en;  // 0-based first/last interior plane per slab
+    // device arrays (FP64)
+    double* U[3];
+    double* Pr;
+    double* PC;
+    double* Q[3];
+    double* Q8;
+    double* RH;      // SSOR forward result (scaled)
+    double* V;       // kmax+1 Krylov vectors, vol each
+    double* uold1;   // U1 at i=1 before the inflow update, (ny, nz)
+    // per-k coefficient arrays and mesh (nz)
+    double *x3, *jacinv, *jac2, *Ab, *At, *Ap, *rAp;
+    // recycling state
+    double *usum2, *vsum2, *wsum2, *wt, *ume1, *bltkns;
+    int* newk;
+    double* ufl_file;  // 3 x (ny,nz) restart-file copy of Ufluc(irec,:,:,:)
+    double* ufl_live;  // 3 x (ny,nz) per-slab live copy
+    double* ufl_full;  // 3 x vol uploaded Ufluc (restart output)
+    double* usum2_fl;  // 3 x (nx,nz): means used by the last per-step Ufluc update
+    // statistics
+    double* sums;      // 9 x (nx,nz): usum vsum wsum uusum vvsum wwsum uvsum uwsum vwsum
+    double* bl_out;    // 4 x nx: deltastar theta Ht Reth
+    double stats_A;    // x2(ny) - x2(2) (dnstbl2/dnstbl.f90:442)
+    std::vector<double> x3h;  // host copy of x3
+    int* slab_of_k;    // nz: slab index of each interior plane
+    tbl::DevScalars* sc;
+    // GMRES small arrays (kmax+1)^2 + 4(kmax+1)
+    double *h, *gg, *gc, *gs, *gy;
+    // reductions
+    tbl::RedWork red;
+    // wavefront
+    double* halo;                  // [2 buffers][3 comps][2 sides][P] planes
+    unsigned long long* flags;     // [3 comps][n_cta]
+    tbl::SweepCta* ctas;           // [n_cta]
+    tbl::SlabDesc* slabs;          // [P]
+    int n_cta;
+    unsigned long long epoch;
+    int* err;                      // device error word
+    // host side
+    double* hpin;                  // pinned readback
+    cudaStream_t stream;
+    int64_t launches;
+    int nstep, cont, nstat;
+    double time;
+    bool fluc_updated;
+    int coop_ok;
+    // replay
+    std::vector<int32_t> replay;
+    size_t replay_pos;
+    std::vector<int32_t> last_counts;
+    double lamda_host;
+};

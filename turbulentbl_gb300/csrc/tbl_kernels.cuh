@@ -1,0 +1,38 @@
+// tbl_kernels.cuh -- host-side launchers shared between translation units.
+#pragma once
+#include "tbl_internal.cuh"
+
+namespace tbl {
+
+// tbl_stencil.cu
+int launch_save_uold(tbl_handle* h);
+int launch_inflow(tbl_handle* h);
+int launch_conv_q(tbl_handle* h);
+int launch_gs_resid(tbl_handle* h, const int* comps, int ncomp, int nblocks);
+int launch_div(tbl_handle* h);
+int launch_pc_zero_faces(tbl_handle* h);
+int launch_project_bcs(tbl_handle* h);
+int launch_div_diag(tbl_handle* h, int nblocks, int slot);
+int launch_fluc_ke(tbl_handle* h, int nblocks, int slot);
+int launch_stats(tbl_handle* h);
+int launch_rescale(tbl_handle* h);
+
+// tbl_sweep.cu
+int build_sweep_ctas(tbl_handle* h);
+int check_cooperative(tbl_handle* h);
+int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity);
+int launch_halo_init(tbl_handle* h, int parity);
+int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8);
+int launch_ssor_bwd(tbl_handle* h, double* out);
+
+// tbl_krylov.cu
+int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);
+int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op);
+int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom);
+int launch_givens(tbl_handle* h, int kit);
+int launch_backsub_update(tbl_handle* h, int kit);
+int launch_restart_init(tbl_handle* h, int first);
+int launch_ppe_resid(tbl_handle* h);
+int red_blocks(tbl_handle* h);
+
+}  // namespace tbl

@@ -1,0 +1,236 @@
+// tbl_krylov.cu -- GMRES(kmax) building blocks in FP64
+// (dnstbl2/dnstbl.f90:952-1208): modified Gram-Schmidt passes with fused
+// grid reductions, normalisation, Givens rotations and back substitution in
+// one device thread, and the solution update p' += V y.
+//
+// Vector kernels stream the whole padded volume: Krylov vectors are zero
+// outside the interior, so boundary and padding entries add nothing to the dot
+// products and stay zero under the updates.
+#include "tbl_internal.cuh"
+#include "tbl_reduce.cuh"
+#include "tbl_kernels.cuh"
+
+namespace tbl {
+
+int red_blocks(tbl_handle* h) {
+    long long n2 = h->g.vol / 2;
+    long long b = (n2 + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+    if (b > h->red.max_blocks) b = h->red.max_blocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// sum(a*b) over the volume -> *out (op 1: sqrt)
+__global__ void __launch_bounds__(RED_THREADS) k_dot(long long n2, const double2* __restrict__ a,
+                                                     const double2* __restrict__ b, RedWork rw, int slot,
+                                                     double* out, int op) {
+    __shared__ double s_red[RED_THREADS / 32];
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += (long long)gridDim.x * blockDim.x) {
+        double2 x = a[q], y = b[q];
+        acc += x.x * y.x;
+        acc += x.y * y.y;
+    }
+    double bt = block_sum(acc, s_red);
+    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
+}
+
+// One modified Gram-Schmidt pass (:1140-1150):
+//   w -= (*hk) * vk          (skipped when vk == nullptr)
+//   *out = sum(vn * w)       (vn == nullptr: sum(w*w), op 1 takes the sqrt)
+__global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __restrict__ w,
+                                                     const double2* __restrict__ vk, const double* __restrict__ hk,
+                                                     const double2* __restrict__ vn, RedWork rw, int slot,
+                                                     double* out, int op) {
+    __shared__ double s_red[RED_THREADS / 32];
+    const double hv = vk ? *hk : 0.0;
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += (long long)gridDim.x * blockDim.x) {
+        double2 x = w[q];
+        if (vk) {
+            double2 v = vk[q];
+            x.x = x.x - hv * v.x;
+            x.y = x.y - hv * v.y;
+            w[q] = x;
+        }
+        double2 y = vn ? vn[q] : x;
+        acc += y.x * x.x;
+        acc += y.y * x.y;
+    }
+    double bt = block_sum(acc, s_red);
+    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
+}
+
+// w /= *denom when *denom != 0 (:1158-1161); multiplies by the reciprocal
+__global__ void k_scale_inv(long long n2, double2* __restrict__ w, const double* __restrict__ denom) {
+    const double d = *denom;
+    if (!(d > 0.0 || d < 0.0)) return;
+    const double r = 1.0 / d;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += (long long)gridDim.x * blockDim.x) {
+        double2 x = w[q];
+        x.x *= r;
+        x.y *= r;
+        w[q] = x;
+    }
+}
+
+// Start of a restart (:958-963, :1048-1056): zero h, c, s, g, y; g(1) = rho;
+// sumnor at the first restart; sumav = rho/sumnor.
+__global__ void k_restart_init(int K1, double* h, double* gg, double* gc, double* gs, double* gy, DevScalars* sc,
+                               int first) {
+    for (int q = threadIdx.x; q < K1 * K1; q += blockDim.x) h[q] = 0.0;
+    for (int q = threadIdx.x; q < K1; q += blockDim.x) { gg[q] = 0.0; gc[q] = 0.0; gs[q] = 0.0; gy[q] = 0.0; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double rho = sc->rho;
+        if (first) sc->sumnor = rho;
+        sc->sumav = rho / sc->sumnor;
+        gg[0] = rho;
+    }
+}
+
+// Givens rotations for column kit (1-based) (:1165-1189).  h(kit+1,kit) holds
+// the norm of the orthogonalised vector; it is saved for the normalisation.
+__global__ void k_givens(int K1, int kit, double* h, double* gg, double* gc, double* gs, DevScalars* sc) {
+    if (threadIdx.x != 0) return;
+    auto H = [&](int a, int b) -> double& { return h[(a - 1) + K1 * (b - 1)]; };
+    sc->red[8] = H(kit + 1, kit);
+    if (kit > 1) {
+        for (int i = 1; i <= kit - 1; ++i) {
+            double hik = gc[i - 1] * H(i, kit) - gs[i - 1] * H(i + 1, kit);
+            double hipk = gs[i - 1] * H(i, kit) + gc[i - 1] * H(i + 1, kit);
+            H(i, kit) = hik;
+            H(i + 1, kit) = hipk;
+        }
+    }
+    double nu = sqrt(H(kit, kit) * H(kit, kit) + H(kit + 1, kit) * H(kit + 1, kit));
+    if (nu > 0.0) {
+        gc[kit - 1] = H(kit, kit) / nu;
+        gs[kit - 1] = -H(kit + 1, kit) / nu;
+        H(kit, kit) = gc[kit - 1] * H(kit, kit) - gs[kit - 1] * H(kit + 1, kit);
+        H(kit + 1, kit) = 0.0;
+        double gk = gc[kit - 1] * gg[kit - 1] - gs[kit - 1] * gg[kit];
+        double gkp = gs[kit - 1] * gg[kit - 1] + gc[kit - 1] * gg[kit];
+        gg[kit - 1] = gk;
+        gg[kit] = gkp;
+    }
+    double rho = fabs(gg[kit]);
+    sc->rho = rho;
+    sc->sumav = rho / sc->sumnor;
+}
+
+// y from the triangular h (:1193-1200), one thread
+__global__ void k_backsub(int K1, int kit, const double* h, const double* gg, double* gy) {
+    if (threadIdx.x != 0) return;
+    auto H = [&](int a, int b) -> double { return h[(a - 1) + K1 * (b - 1)]; };
+    gy[kit - 1] = gg[kit - 1] / H(kit, kit);
+    for (int i = kit - 1; i >= 1; --i) {
+        double yi = gg[i - 1];
+        for (int k = i + 1; k <= kit; ++k) yi = yi - H(i, k) * gy[k - 1];
+        gy[i - 1] = yi / H(i, i);
+    }
+}
+
+// p' += sum_i v_i y_i, accumulated in the reference's order (:1202-1205)
+__global__ void k_update(long long n2, double2* __restrict__ pc, const double2* __restrict__ V, long long vstride2,
+                         const double* __restrict__ gy, int kit) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += (long long)gridDim.x * blockDim.x) {
+        double2 x = pc[q];
+        for (int i = 0; i < kit; ++i) {
+            double2 v = V[(long long)i * vstride2 + q];
+            double y = gy[i];
+            x.x = x.x + v.x * y;
+            x.y = x.y + v.y * y;
+        }
+        pc[q] = x;
+    }
+}
+
+// ||L7 p' - Q8||^2 and ||Q8||^2 over the interior -> red[9], red[10]
+__global__ void __launch_bounds__(RED_THREADS) k_ppe_resid(Geom g, double aw, double as, const double* __restrict__ Ab,
+                                                           const double* __restrict__ At, const double* __restrict__ Ap,
+                                                           const double* __restrict__ PC, const double* __restrict__ Q8,
+                                                           RedWork rw, DevScalars* sc) {
+    __shared__ double s_red[RED_THREADS / 32];
+    const int ni = g.nx - 2, J = g.ny - 2, nk = g.nz - 2;
+    const long long n = (long long)ni * J * nk;
+    double num = 0.0, den = 0.0;
+    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += (long long)gridDim.x * blockDim.x) {
+        int i = 1 + (int)(t0 % ni);
+        long long r = t0 / ni;
+        int j = 1 + (int)(r % J);
+        int k = 1 + (int)(r / J);
+        long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
+        int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
+        long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
+        long long pjp = (long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k);
+        double lap = aw * PC[p - 1] + aw * PC[p + 1] + as * PC[pjm] + as * PC[pjp] + Ab[k] * PC[p - g.ps] +
+                     At[k] * PC[p + g.ps] + Ap[k] * PC[p];
+        double rr = lap - Q8[p];
+        num += rr * rr;
+        den += Q8[p] * Q8[p];
+    }
+    double b1 = block_sum(num, s_red);
+    __syncthreads();
+    double b2 = block_sum(den, s_red);
+    grid_finish(b1, rw, 9, gridDim.x, blockIdx.x, &sc->red[9], 0);
+    __syncthreads();
+    grid_finish(b2, rw, 10, gridDim.x, blockIdx.x, &sc->red[10], 0);
+}
+
+// ------------------------------------------------------------- host glue
+int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op) {
+    int nb = red_blocks(h);
+    k_dot<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (const double2*)a, (const double2*)b, h->red, 7, out, op);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op) {
+    int nb = red_blocks(h);
+    k_mgs<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, (const double2*)vk, hk, (const double2*)vn,
+                                             h->red, 7, out, op);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom) {
+    int nb = red_blocks(h);
+    k_scale_inv<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, denom);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_restart_init(tbl_handle* h, int first) {
+    const int K1 = h->cfg.kmax + 1;
+    k_restart_init<<<1, 256, 0, h->stream>>>(K1, h->h, h->gg, h->gc, h->gs, h->gy, h->sc, first);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_givens(tbl_handle* h, int kit) {
+    const int K1 = h->cfg.kmax + 1;
+    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_backsub_update(tbl_handle* h, int kit) {
+    const int K1 = h->cfg.kmax + 1;
+    k_backsub<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gy);
+    int nb = red_blocks(h);
+    k_update<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)h->PC, (const double2*)h->V, h->g.vol / 2,
+                                                h->gy, kit);
+    h->launches += 2;
+    return TBL_OK;
+}
+
+int launch_ppe_resid(tbl_handle* h) {
+    int nb = red_blocks(h);
+    k_ppe_resid<<<nb, RED_THREADS, 0, h->stream>>>(h->g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy),
+                                                   h->Ab, h->At, h->Ap, h->PC, h->Q8, h->red, h->sc);
+    h->launches++;
+    return TBL_OK;
+}
+
+}  // namespace tbl
