@@ -70,7 +70,7 @@ def _smooth_noise(rng, shape, width):
     K = np.meshgrid(*ks, indexing="ij")
     k2 = sum(k * k for k in K)
     F *= np.exp(-2.0 * (np.pi * width) ** 2 * k2)
-    return np.fft.irfftn(F, s=shape)
+    return np.fft.irfftn(F, s=shape, axes=tuple(range(len(shape))))
 
 
 def _ddx(f, h, axis):
