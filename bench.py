@@ -1,0 +1,317 @@
+"""Benchmark of the turbulentBL time step on GB300.
+
+Headline: grid-point-steps per second (Mpt-steps/s) of the plain FP64 method
+on the 512 x 128 x 128 seeded box (nx x ny_wall x nz_span; reference arrays
+n3d = (512, 130, 128)), GMRES restart 40, tol 1e-10, P = 8 virtual slabs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One "step" is one full time step of the reference time loop (inflow,
+convection, implicit diffusion, pressure-Poisson GMRES, projection, BCs,
+statistics and the every-cum rescaling).  Fields are 68-400 MB each, far above
+the 129 MB L2, so no cache flush is needed between steps.
+
+Arms:
+  ours       libtblgpu.so on cuda:LOCAL_RANK.  `value` is device-timed (CUDA
+             events around K steps, inputs resident); `e2e` drives K further
+             steps through the C ABI with pinned host buffers: each step uploads
+             u, v, w, p, p' and downloads u, v, w, p.
+  reference  the CPU restatement of the reference (oracle/, C++ FP64 with P
+             virtual MPI ranks, OpenMP over all host cores) on the same
+             workload; steps run from the seeded field until a time budget is
+             used (at least one full step).  The reference Fortran/MPI program
+             cannot be built on these machines (no Fortran compiler, no MPI).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from turbulentbl_gb300 import abi  # noqa: E402
+from turbulentbl_gb300.synth import WORKLOADS, make_state  # noqa: E402
+
+FALLBACK_HBM_GBS = 6800.0
+FP64_PEAK_TFLOPS = 1.2  # measured FMA throughput on this machine's GB300 (FP64 is 1/64 of FP32)
+
+GROUP_NAMES = ["conv_q", "gs_sweep", "gs_resid", "ssor_fwd_matvec", "ssor_bwd", "mgs", "small", "vec", "bc", "stats",
+               "total"]
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM traffic of the kernel groups from a committed ncu summary."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_cpu(wl, nproc, budget_s, max_steps):
+    """Time the oracle (all host threads) from the seeded field for up to max_steps steps
+    or until budget_s seconds are used; at least one step."""
+    from oracle.bind import OracleRunner
+    mesh, rp, st = make_state(wl, nproc=nproc)
+    o = OracleRunner(mesh, rp)
+    o.upload(st)
+    times, counts = [], []
+    t_all = time.perf_counter()
+    while len(times) < max(1, max_steps):
+        t0 = time.perf_counter()
+        o.step(1, check=False)
+        times.append(time.perf_counter() - t0)
+        counts.append(o.last_counts())
+        if time.perf_counter() - t_all > budget_s:
+            break
+    threads = os.cpu_count() or 1
+    mean_t = float(np.sum(times)) / len(times)
+    value = wl.points / mean_t / 1e6
+    iters = [int(np.sum(c[4:])) for c in counts]
+    return {
+        "value": value, "unit": "Mpt-steps/s", "cores": threads, "kind": "port",
+        "sample": (f"{len(times)} full time step(s) of {wl.name} from the seeded field "
+                   f"(steps 1..{len(times)}), C++ FP64 restatement with P={nproc} virtual ranks, "
+                   f"OpenMP {threads} threads; GMRES Arnoldi iterations per step {iters}, "
+                   f"GS sweeps per step {[c[:3] for c in counts]}"),
+        "s_per_step": mean_t,
+    }
+
+
+def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget):
+    import torch
+    torch.cuda.set_device(local)
+    from turbulentbl_gb300.lib import TblGpu
+    mesh, rp, st = make_state(wl, nproc=nproc)
+    g = TblGpu(mesh, rp)
+    g.upload(st)
+    for _ in range(warmup):
+        g.step(1, check=False)
+    L = g.lib
+    L.tbl_profile.argtypes = [abi.C.c_void_p, abi.C.c_int]
+    L.tbl_profile_read.argtypes = [abi.C.c_void_p, abi.C.POINTER(abi.C.c_double), abi.C.POINTER(abi.C.c_double),
+                                   abi.C.POINTER(abi.C.c_int64), abi.C.c_int]
+    L.tbl_profile(g._h, 1)
+    launches0 = g.launches()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.4)
+    torch.cuda.synchronize()
+    # device time: CUDA events recorded by the library on its own stream
+    # around the K steps (tbl_profile group "total"); host time alongside
+    e0 = time.perf_counter()
+    st_all, recs = g.step(steps, check=False)
+    torch.cuda.synchronize()
+    e1 = time.perf_counter()
+    ng = len(GROUP_NAMES)
+    ms = (abi.C.c_double * ng)()
+    by = (abi.C.c_double * ng)()
+    nl = (abi.C.c_int64 * ng)()
+    L.tbl_profile_read(g._h, ms, by, nl, ng)
+    dev_elapsed = ms[ng - 1] * 1e-3
+    if world > 1:
+        t = torch.tensor([dev_elapsed], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    else:
+        elapsed = dev_elapsed
+    clk = clocks.stop()
+    launches = g.launches() - launches0
+    L.tbl_profile(g._h, 0)
+    groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launch_groups": nl[q]} for q in range(ng - 1)}
+    out = {"elapsed": elapsed, "host_elapsed": e1 - e0, "recs": recs, "status": st_all, "launches": launches,
+           "clocks": clk, "groups": groups}
+    if do_e2e:
+        nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
+        n = nx * ny * nz
+        host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in ("u", "v", "w", "p", "pcorr")}
+        d = g.download(fields=("u", "v", "w", "p", "pcorr"))
+        for f in host:
+            host[f][:] = np.asarray(d[f], order="F").reshape(-1, order="F")
+        L.tbl_upload_fields.argtypes = [abi.C.c_void_p] + [abi.C.POINTER(abi.C.c_double)] * 5
+        S = abi.TblState()
+        for f in ("u", "v", "w", "p"):
+            setattr(S, f, host[f].ctypes.data_as(abi.C.POINTER(abi.C.c_double)))
+        ptr = {f: host[f].ctypes.data_as(abi.C.POINTER(abi.C.c_double)) for f in host}
+        arr = (abi.TblStepStats * 1)()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        e2e_recs = []
+        for _ in range(steps):
+            L.tbl_upload_fields(g._h, ptr["u"], ptr["v"], ptr["w"], ptr["p"], ptr["pcorr"])
+            L.tbl_step(g._h, 1, arr)
+            e2e_recs.append(arr[0].as_dict())
+            L.tbl_download_state(g._h, abi.C.byref(S))
+        t1 = time.perf_counter()
+        te = t1 - t0
+        if world > 1:
+            t = torch.tensor([te], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            te = float(t.item())
+        out["e2e"] = {"elapsed": te, "h2d": 5 * n * 8, "d2h": 4 * n * 8,
+                      "iters": [r["gmres_iters"] for r in e2e_recs]}
+    g.close()
+    if do_cpu and rank == 0:
+        out["cpu"] = run_cpu(wl, nproc, cpu_budget, 1)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="box512_fp64", choices=sorted(WORKLOADS))
+    ap.add_argument("--nproc", type=int, default=8, help="virtual MPI ranks (slabs)")
+    ap.add_argument("--cpu-budget", type=float, default=30.0, help="seconds of CPU time for the CPU sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    wl = WORKLOADS[args.workload]
+    dtype = "f64" if wl.precision == 0 else "f32+f64"
+    config = {"workload": wl.name, "grid_nx_ny_nz": [wl.nx, wl.ny_wall, wl.nz_span],
+              "reference_n3d": list(wl.n3d), "virtual_ranks": args.nproc, "gmres_restart": wl.kmax,
+              "gmres_tol": wl.errtol, "re_theta": wl.re_theta, "cfl": wl.cfl, "seed": wl.seed,
+              "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+              "l2": "inputs larger than L2 (fields 68 MB+, Krylov basis 2.8 GB)"}
+    metric = "Mpt-steps/s"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu = run_cpu(wl, args.nproc, max(args.cpu_budget, 1.0) * max(args.steps, 1), args.steps)
+        line = {"metric": metric, "value": cpu["value"], "unit": "Mpt-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": 0, "ms_per_step": cpu["s_per_step"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)",
+                "config": config, "impl": "reference",
+                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cpu["value"], "unit": "Mpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
+                not args.no_cpu, args.cpu_budget)
+    if rank != 0:
+        return
+    K = args.steps
+    value = wl.points * K * world / r["elapsed"] / 1e6
+    hbm, hbm_kind = peaks()
+    groups = r["groups"]
+    top = max(groups, key=lambda k: groups[k]["ms"])
+    tg = groups[top]
+    launches_top = tg["launch_groups"]
+    achieved = tg["bytes"] / (tg["ms"] * 1e-3) / 1e9 if tg["ms"] > 0 else 0.0
+    traffic = traffic_table().get(top)
+    roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": traffic, "share_of_step": tg["ms"] / (r["elapsed"] * 1e3),
+                "per_launch_ms": tg["ms"] / max(launches_top, 1)}
+    step_bytes = sum(v["bytes"] for v in groups.values())
+    line = {"metric": metric, "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": K,
+            "warmup": max(args.warmup, 3), "ms_per_step": r["elapsed"] * 1e3 / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded 1/7-law + curl noise)",
+            "config": config, "roofline": roofline,
+            "step_hbm": {"algorithmic_gb_per_step": step_bytes / K / 1e9,
+                         "achieved_gbs": step_bytes / r["elapsed"] / 1e9, "frac": step_bytes / r["elapsed"] / 1e9 / hbm},
+            "groups_ms_per_step": {k: v["ms"] / K for k, v in groups.items()},
+            "gmres_iters_per_step": [x["gmres_iters"] for x in r["recs"]],
+            "gs_sweeps_per_step": [x["gs_sweeps"] for x in r["recs"]],
+            "status": abi.STATUS_NAMES.get(r["status"], r["status"]),
+            "host_ms_per_step": r["host_elapsed"] * 1e3 / K,
+            "gpu_launches": r["launches"], "clocks": r["clocks"]}
+    if "e2e" in r:
+        e = r["e2e"]
+        line["e2e"] = {"value": wl.points * K * world / e["elapsed"] / 1e6, "unit": "Mpt-steps/s",
+                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
+                       "gmres_iters_per_step": e["iters"]}
+    if "cpu" in r:
+        c = r["cpu"]
+        line["cpu_baseline"] = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

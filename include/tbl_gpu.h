@@ -173,6 +173,32 @@ int tbl_set_replay(tbl_handle* h, const int32_t* rec, int64_t len);
  * Returns the record length (>= 4) or a negative status; writes at most cap. */
 int tbl_last_counts(tbl_handle* h, int32_t* buf, int32_t cap);
 
+/* Replace only the 3-D fields (u, v, w, p and, when non-NULL, pcorr) and keep
+ * the recycling state, statistics accumulators and step counters: the
+ * per-step entry of a host driver that owns Ut/Press/PCorr in its own arrays
+ * (the reference's program-global arrays, dnstbl2/dnstbl.f90:172-321). */
+int tbl_upload_fields(tbl_handle* h, const double* u, const double* v, const double* w, const double* p,
+                      const double* pcorr);
+
+/* Kernel-group timing with CUDA events on the library's stream.  enable=1
+ * turns it on (and clears the totals), 0 turns it off.  tbl_profile_read
+ * copies per-group totals: milliseconds, algorithmic bytes and launches, for
+ * TBL_PROF_NGROUPS groups (indices TBL_PROF_*). */
+#define TBL_PROF_CONV      0  /* convection + explicit RHS */
+#define TBL_PROF_GS_SWEEP  1  /* GS wavefront sweeps */
+#define TBL_PROF_GS_RESID  2  /* GS residual checks */
+#define TBL_PROF_SSOR_FWD  3  /* fused L7 matvec + forward SSOR sweep */
+#define TBL_PROF_SSOR_BWD  4  /* backward SSOR sweep */
+#define TBL_PROF_MGS       5  /* Gram-Schmidt passes with fused reductions */
+#define TBL_PROF_SMALL     6  /* Givens / back substitution / restart set-up */
+#define TBL_PROF_VEC       7  /* normalisation and p' update */
+#define TBL_PROF_BC        8  /* divergence, projection, boundary conditions */
+#define TBL_PROF_STATS     9  /* statistics, diagnostics, rescaling */
+#define TBL_PROF_TOTAL    10  /* whole tbl_step calls, device time between events on the stream */
+#define TBL_PROF_NGROUPS  11
+int tbl_profile(tbl_handle* h, int enable);
+int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches, int ngroups);
+
 /* Release everything. */
 void tbl_destroy(tbl_handle* h);
 

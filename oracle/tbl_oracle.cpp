@@ -213,6 +213,7 @@ void conv_q(Oracle& o) {
         const std::vector<double>& U1 = o.U[0];
         const std::vector<double>& U2 = o.U[1];
         const std::vector<double>& U3 = o.U[2];
+#pragma omp parallel for schedule(static)
         for (int k = 2; k <= nz - 1; ++k)
             for (int j = 2; j <= ny - 1; ++j)
                 for (int i = 2; i <= nx - 1; ++i) {
@@ -283,6 +284,7 @@ void conv_q(Oracle& o) {
                 }
     }
     // Q (:719-768); forc = 0, Ri = 0
+#pragma omp parallel for schedule(static)
     for (int k = 2; k <= nz - 1; ++k)
         for (int j = 2; j <= ny - 1; ++j)
             for (int i = 2; i <= nx - 1; ++i) {
@@ -316,6 +318,8 @@ void gs_solve(Oracle& o, int replay_sweeps[3], int out_sweeps[3], double out_res
             if (it % 2 == 1) {
                 // residual with current halos (:781-828)
                 double diver = 0.0;
+                std::vector<double> part(o.P, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
                 for (int rk = 0; rk < o.P; ++rk) {
                     double tmp = 0.0;
                     for (int k = o.bn[rk]; k <= o.en[rk]; ++k) {
@@ -329,8 +333,9 @@ void gs_solve(Oracle& o, int replay_sweeps[3], int out_sweeps[3], double out_res
                                 tmp = tmp + std::fabs(res);
                             }
                     }
-                    diver += tmp;  // allreduce in rank order
+                    part[rk] = tmp;
                 }
+                for (int rk = 0; rk < o.P; ++rk) diver += part[rk];  // allreduce in rank order
                 if (it == 1) sumnor = 1.0 / diver;
                 sumav = diver * sumnor;
                 bool stop = replay ? (sweeps >= replay_sweeps[jc]) : (sumav < o.c.errorstop);
@@ -342,6 +347,7 @@ void gs_solve(Oracle& o, int replay_sweeps[3], int out_sweeps[3], double out_res
                 if (rk < o.P - 1) std::memcpy(&o.snap_hi[rk * plane], &F[o.id(1, 1, o.en[rk] + 1)], plane * sizeof(double));
             }
             // lexicographic sweep per slab (:830-868), halos from the snapshot
+#pragma omp parallel for schedule(dynamic, 1)
             for (int rk = 0; rk < o.P; ++rk) {
                 const double* lo = &o.snap_lo[rk * plane];
                 const double* hi = &o.snap_hi[rk * plane];
@@ -370,6 +376,7 @@ void gs_solve(Oracle& o, int replay_sweeps[3], int out_sweeps[3], double out_res
 // dnstbl2/dnstbl.f90:905-935
 void divergence(Oracle& o) {
     const int nx = o.nx, ny = o.ny, nz = o.nz;
+#pragma omp parallel for schedule(static)
     for (int k = 2; k <= nz - 1; ++k)
         for (int j = 2; j <= ny - 1; ++j)
             for (int i = 2; i <= nx - 1; ++i) {
@@ -400,6 +407,7 @@ void ssor(Oracle& o, const std::vector<double>& in) {
     const double w = o.c.omega;
     const double scale_w = (2 - w) / w;
     std::fill(o.rhat.begin(), o.rhat.end(), 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rk = 0; rk < o.P; ++rk) {
         auto R = [&](int i, int j, int k) -> double {
             if (i < 2 || i > nx - 1 || j < 2 || j > ny - 1 || k < o.bn[rk] || k > o.en[rk]) return 0.0;
@@ -426,13 +434,16 @@ void ssor(Oracle& o, const std::vector<double>& in) {
 // sum over the interior of all slabs of a*b: per-rank partial, rank order
 double dot(const Oracle& o, const std::vector<double>& a, const std::vector<double>& b) {
     double tot = 0.0;
+    std::vector<double> part(o.P, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rk = 0; rk < o.P; ++rk) {
         double s = 0.0;
         for (int k = o.bn[rk]; k <= o.en[rk]; ++k)
             for (int j = 2; j <= o.ny - 1; ++j)
                 for (int i = 2; i <= o.nx - 1; ++i) s = s + a[o.id(i, j, k)] * b[o.id(i, j, k)];
-        tot += s;
+        part[rk] = s;
     }
+    for (int rk = 0; rk < o.P; ++rk) tot += part[rk];
     return tot;
 }
 
@@ -459,11 +470,13 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
         std::fill(o.cs.begin(), o.cs.end(), 0.0); std::fill(o.sn.begin(), o.sn.end(), 0.0);
         std::fill(o.g.begin(), o.g.end(), 0.0); std::fill(o.y.begin(), o.y.end(), 0.0);
         // r = Q8 - L7 PCorr (:995-1008)
+#pragma omp parallel for schedule(static)
         for (int k = 2; k <= nz - 1; ++k)
             for (int j = 2; j <= ny - 1; ++j)
                 for (int i = 2; i <= nx - 1; ++i)
                     o.r[o.id(i, j, k)] = o.Q8[o.id(i, j, k)] - (lap(o, o.PC, i, j, k));
         ssor(o, o.r);
+#pragma omp parallel for schedule(static)
         for (int k = 2; k <= nz - 1; ++k)
             for (int j = 2; j <= ny - 1; ++j)
                 for (int i = 2; i <= nx - 1; ++i) o.r[o.id(i, j, k)] = o.rhat[o.id(i, j, k)];
@@ -474,6 +487,7 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
         }
         sumav = rho / sumnor;
         o.g[0] = rho;
+#pragma omp parallel for schedule(static)
         for (int k = 2; k <= nz - 1; ++k)
             for (int j = 2; j <= ny - 1; ++j)
                 for (int i = 2; i <= nx - 1; ++i) o.V[0][o.id(i, j, k)] = o.r[o.id(i, j, k)] / rho;
@@ -483,11 +497,13 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
             kit = kit + 1;
             std::vector<double>& vk = o.V[kit - 1];
             std::vector<double>& vn = o.V[kit];
-            for (int k = 2; k <= nz - 1; ++k)
+    #pragma omp parallel for schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
                 for (int j = 2; j <= ny - 1; ++j)
                     for (int i = 2; i <= nx - 1; ++i) vn[o.id(i, j, k)] = lap(o, vk, i, j, k);
             ssor(o, vn);
-            for (int k = 2; k <= nz - 1; ++k)
+    #pragma omp parallel for schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
                 for (int j = 2; j <= ny - 1; ++j)
                     for (int i = 2; i <= nx - 1; ++i) vn[o.id(i, j, k)] = o.rhat[o.id(i, j, k)];
             // modified Gram-Schmidt (:1140-1150)
@@ -495,14 +511,16 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
                 H(kk, kit) = dot(o, o.V[kk - 1], vn);
                 double hk = H(kk, kit);
                 const std::vector<double>& vv = o.V[kk - 1];
-                for (int k = 2; k <= nz - 1; ++k)
+        #pragma omp parallel for schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
                     for (int j = 2; j <= ny - 1; ++j)
                         for (int i = 2; i <= nx - 1; ++i) vn[o.id(i, j, k)] = vn[o.id(i, j, k)] - hk * vv[o.id(i, j, k)];
             }
             H(kit + 1, kit) = std::sqrt(dot(o, vn, vn));
             if (H(kit + 1, kit) > 0.0 || H(kit + 1, kit) < 0.0) {
                 double hh = H(kit + 1, kit);
-                for (int k = 2; k <= nz - 1; ++k)
+        #pragma omp parallel for schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
                     for (int j = 2; j <= ny - 1; ++j)
                         for (int i = 2; i <= nx - 1; ++i) vn[o.id(i, j, k)] = vn[o.id(i, j, k)] / hh;
             }
@@ -543,7 +561,8 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
         for (int i = 1; i <= kit; ++i) {
             const std::vector<double>& vv = o.V[i - 1];
             double yi = o.y[i - 1];
-            for (int k = 2; k <= nz - 1; ++k)
+    #pragma omp parallel for schedule(static)
+        for (int k = 2; k <= nz - 1; ++k)
                 for (int j = 2; j <= ny - 1; ++j)
                     for (int ii = 2; ii <= nx - 1; ++ii)
                         o.PC[o.id(ii, j, k)] = o.PC[o.id(ii, j, k)] + vv[o.id(ii, j, k)] * yi;
@@ -580,6 +599,7 @@ void project_bcs(Oracle& o) {
             PC[o.id(nx, j, k)] = (5.0 * PC[o.id(nx - 1, j, k)] + (-4.0 * PC[o.id(nx - 2, j, k)] + PC[o.id(nx - 3, j, k)])) / 2.0;
     // P += p' (:1268), U -= dt grad p' (:1271-1314)
     const double dt = o.c.dt;
+#pragma omp parallel for schedule(static)
     for (int k = 2; k <= nz - 1; ++k)
         for (int j = 2; j <= ny - 1; ++j)
             for (int i = 2; i <= nx - 1; ++i) {
@@ -733,6 +753,7 @@ void per_step_stats(Oracle& o, double& ke, int& blowup) {
         o.nstat += 1;
         const double dA = o.dy;
         const double A = o.x2[ny - 1] - o.x2[1];
+#pragma omp parallel for schedule(static)
         for (int i = 1; i <= nx; ++i)
             for (int k = 1; k <= nz; ++k) {
                 double su_, sv_, sw_, tu = 0, tv = 0, tw = 0, tuu = 0, tvv = 0, tww = 0, tuv = 0, tuw = 0, tvw = 0;

@@ -18,6 +18,43 @@ void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int 
     snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
 }
 
+static int take_event(tbl_handle* h) {
+    if (h->prof_used == h->prof_ev.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
+        h->prof_ev.push_back(e);
+    }
+    return (int)h->prof_used++;
+}
+
+ProfScope::ProfScope(tbl_handle* h_, int g_, double b_) : h(h_), group(g_), bytes(b_), e0(-1) {
+    if (!h->prof_on) return;
+    e0 = take_event(h);
+    if (e0 >= 0) cudaEventRecord(h->prof_ev[e0], h->stream);
+}
+
+ProfScope::~ProfScope() {
+    if (!h->prof_on || e0 < 0) return;
+    int e1 = take_event(h);
+    if (e1 < 0) return;
+    cudaEventRecord(h->prof_ev[e1], h->stream);
+    h->prof_marks.push_back({group, e0, e1, bytes});
+}
+
+// Accumulates the recorded event pairs (the stream must be idle).
+int prof_drain(tbl_handle* h) {
+    for (const auto& m : h->prof_marks) {
+        float ms = 0.f;
+        TBL_CUDA_TRY(cudaEventElapsedTime(&ms, h->prof_ev[m.e0], h->prof_ev[m.e1]));
+        h->prof_ms[m.group] += ms;
+        h->prof_bytes[m.group] += m.bytes;
+        h->prof_n[m.group] += 1;
+    }
+    h->prof_marks.clear();
+    h->prof_used = 0;
+    return TBL_OK;
+}
+
 static int readback(tbl_handle* h, const void* dev, size_t bytes) {
     TBL_CUDA_TRY(cudaMemcpyAsync(h->hpin, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -60,6 +97,7 @@ static void free_all(tbl_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->hpin) cudaFreeHost(h->hpin);
+    for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -72,6 +110,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     g.ps = (long long)g.sx * ny;
     g.vol = g.ps * nz;
     g.J = ny - 2;
+    h->npts = (double)nx * ny * nz;
     h->P = cfg->nproc;
     const int loc_n = (nz - 1) / h->P;  // (:469-475), 1-based bn = 2 + r*loc_n
     h->bn.resize(h->P);
@@ -160,7 +199,10 @@ static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
         for (int c = 0; c < 3; ++c)
             if (active[c]) comps[n++] = c;
         if (it % 2 == 1) {  // residual check every other sweep (:781-828)
-            TRY(launch_gs_resid(h, comps, n, nb > 512 ? 512 : nb));
+            {
+                ProfScope ps(h, TBL_PROF_GS_RESID, 2.0 * 8.0 * h->npts * n);
+                TRY(launch_gs_resid(h, comps, n, nb > 512 ? 512 : nb));
+            }
             TRY(readback(h, &h->sc->red[0], 3 * sizeof(double)));
             const double* red = h->hpin;
             int m = 0;
@@ -176,7 +218,10 @@ static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
             n = m;
             if (n == 0) break;
         }
-        TRY(launch_gs_sweep(h, comps, n, parity));
+        {
+            ProfScope ps(h, TBL_PROF_GS_SWEEP, 3.0 * 8.0 * h->npts * n);
+            TRY(launch_gs_sweep(h, comps, n, parity));
+        }
         parity ^= 1;
         for (int q = 0; q < n; ++q) sweeps[comps[q]]++;
     }
@@ -195,35 +240,68 @@ static int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, 
     while (rec ? (m < nr) : ((sumav > h->cfg.errtol) && (m < h->cfg.mmax))) {
         m = m + 1;
         double* V0 = h->V;
-        TRY(launch_ssor_fwd(h, h->PC, h->Q8));  // r = Q8 - L7 p', then SSOR (:995-1042)
-        TRY(launch_ssor_bwd(h, V0));
-        TRY(launch_dot(h, V0, V0, &h->sc->rho, 1));
+        const double wN = 8.0 * h->npts;
+        {
+            ProfScope ps(h, TBL_PROF_SSOR_FWD, 3.0 * wN);
+            TRY(launch_ssor_fwd(h, h->PC, h->Q8));  // r = Q8 - L7 p', then SSOR (:995-1042)
+        }
+        {
+            ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
+            TRY(launch_ssor_bwd(h, V0));
+        }
+        {
+            ProfScope ps(h, TBL_PROF_MGS, 1.0 * wN);
+            TRY(launch_dot(h, V0, V0, &h->sc->rho, 1));
+        }
         TRY(launch_restart_init(h, m == 1));
         TRY(readback(h, &h->sc->rho, 4 * sizeof(double)));  // rho, sumnor, sumav
         double rho = h->hpin[0];
         if (m == 1 && !(rho > 0.0)) { status = TBL_ERR_ZERO_RHS; break; }
         sumav = h->hpin[2];
-        TRY(launch_scale_by_inv(h, V0, &h->sc->rho));
+        {
+            ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
+            TRY(launch_scale_by_inv(h, V0, &h->sc->rho));
+        }
         int kit = 0;
         const int target = rec ? rec[m] : 0;
         while (rec ? (kit < target) : ((sumav > h->cfg.errtol) && (kit < kmax))) {
             kit = kit + 1;
             double* W = h->V + (size_t)kit * vol;
-            TRY(launch_ssor_fwd(h, h->V + (size_t)(kit - 1) * vol, nullptr));
-            TRY(launch_ssor_bwd(h, W));
+            {
+                ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN);
+                TRY(launch_ssor_fwd(h, h->V + (size_t)(kit - 1) * vol, nullptr));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
+                TRY(launch_ssor_bwd(h, W));
+            }
             double* hcol = h->h + (size_t)K1 * (kit - 1);
-            TRY(launch_mgs(h, W, nullptr, nullptr, V0, &hcol[0], 0));
-            for (int kk = 1; kk <= kit - 1; ++kk)
-                TRY(launch_mgs(h, W, h->V + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->V + (size_t)kk * vol, &hcol[kk], 0));
-            TRY(launch_mgs(h, W, h->V + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
-            TRY(launch_givens(h, kit));
-            TRY(launch_scale_by_inv(h, W, &h->sc->red[8]));
+            {
+                // passes: <v1,w>; (kit-1) x {w -= h v_k; <v_k+1,w>}; w -= h v_kit, ||w||
+                ProfScope ps(h, TBL_PROF_MGS, (2.0 + 4.0 * (kit - 1) + 3.0) * wN);
+                TRY(launch_mgs(h, W, nullptr, nullptr, V0, &hcol[0], 0));
+                for (int kk = 1; kk <= kit - 1; ++kk)
+                    TRY(launch_mgs(h, W, h->V + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->V + (size_t)kk * vol,
+                                   &hcol[kk], 0));
+                TRY(launch_mgs(h, W, h->V + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_SMALL, 0.0);
+                TRY(launch_givens(h, kit));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
+                TRY(launch_scale_by_inv(h, W, &h->sc->red[8]));
+            }
             TRY(readback(h, &h->sc->sumav, sizeof(double)));
             sumav = h->hpin[0];
         }
         iters += kit;
         kits.push_back(kit);
-        if (kit > 0) TRY(launch_backsub_update(h, kit));
+        if (kit > 0) {
+            ProfScope ps(h, TBL_PROF_VEC, (kit + 2.0) * wN);
+            TRY(launch_backsub_update(h, kit));
+        }
     }
     st.gmres_restarts = m;
     st.gmres_iters = iters;
@@ -250,12 +328,22 @@ static int one_step(tbl_handle* h, tbl_step_stats* out) {
         rec = r + 3;
         h->replay_pos += 4 + r[3];
     }
-    TRY(launch_save_uold(h));
-    if (h->nstep > c.recycle_after) TRY(launch_inflow(h));
-    TRY(launch_conv_q(h));
+    const double wN = 8.0 * h->npts;
+    {
+        ProfScope ps(h, TBL_PROF_BC, 0.0);
+        TRY(launch_save_uold(h));
+        if (h->nstep > c.recycle_after) TRY(launch_inflow(h));
+    }
+    {
+        ProfScope ps(h, TBL_PROF_CONV, 7.0 * wN);
+        TRY(launch_conv_q(h));
+    }
     TRY(gs_solve(h, replay ? gs_target : nullptr, st));
-    TRY(launch_div(h));
-    TRY(launch_pc_zero_faces(h));
+    {
+        ProfScope ps(h, TBL_PROF_BC, 4.0 * wN);
+        TRY(launch_div(h));
+        TRY(launch_pc_zero_faces(h));
+    }
     std::vector<int32_t> kits;
     int status = gmres(h, rec, kits, st);
     if (status == TBL_ERR_ZERO_RHS || status < 0 && status != TBL_ERR_NOT_CONVERGED) return status;
@@ -264,30 +352,37 @@ static int one_step(tbl_handle* h, tbl_step_stats* out) {
         TRY(readback(h, &h->sc->red[9], 2 * sizeof(double)));
         st.ppe_rel_resid = h->hpin[1] > 0 ? std::sqrt(h->hpin[0] / h->hpin[1]) : 0.0;
     }
-    TRY(launch_project_bcs(h));
+    {
+        ProfScope ps(h, TBL_PROF_BC, 9.0 * wN);
+        TRY(launch_project_bcs(h));
+    }
     const int nb = red_blocks(h);
-    TRY(launch_div_diag(h, nb > 512 ? 512 : nb, 3));
     const bool fluc = h->nstep > c.recycle_after;
-    if (fluc) {
-        TRY(launch_fluc_ke(h, nb > 512 ? 512 : nb, 4));
-        const size_t n2 = (size_t)c.nx * c.nz;
-        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl, h->usum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
-        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + n2, h->vsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
-        TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + 2 * n2, h->wsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
-        h->fluc_updated = true;
-    }
-    h->cont = h->cont + 1;
-    if (h->nstep % c.istat == 0) {
-        TRY(launch_stats(h));
-        h->nstat++;
-    }
-    st.cum_step = 0;
-    if (h->cont % c.cum == 0) {
-        TRY(launch_rescale(h));
-        st.cum_step = 1;
+    {
+        ProfScope ps_stats(h, TBL_PROF_STATS, (fluc ? 9.0 : 6.0) * wN);
+        TRY(launch_div_diag(h, nb > 512 ? 512 : nb, 3));
+        if (fluc) {
+            TRY(launch_fluc_ke(h, nb > 512 ? 512 : nb, 4));
+            const size_t n2 = (size_t)c.nx * c.nz;
+            TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl, h->usum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+            TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + n2, h->vsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+            TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + 2 * n2, h->wsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
+            h->fluc_updated = true;
+        }
+        h->cont = h->cont + 1;
+        if (h->nstep % c.istat == 0) {
+            TRY(launch_stats(h));
+            h->nstat++;
+        }
+        st.cum_step = 0;
+        if (h->cont % c.cum == 0) {
+            TRY(launch_rescale(h));
+            st.cum_step = 1;
+        }
     }
     // scalars back: red[3] div, red[4] KE, red[5] max fluct, lamda, err
     TRY(readback(h, h->sc, sizeof(DevScalars)));
+    if (h->prof_on) TRY(prof_drain(h));
     DevScalars sc;
     memcpy(&sc, h->hpin, sizeof(sc));
     int err = 0;
@@ -400,8 +495,38 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
     return TBL_OK;
 }
 
-int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
-    if (!h || nsteps < 0) return TBL_ERR_BAD_ARG;
+int tbl_upload_fields(tbl_handle* h, const double* u, const double* v, const double* w, const double* p,
+                      const double* pcorr) {
+    if (!h || !u || !v || !w || !p) return TBL_ERR_BAD_ARG;
+    TRY(put3(h, h->U[0], u));
+    TRY(put3(h, h->U[1], v));
+    TRY(put3(h, h->U[2], w));
+    TRY(put3(h, h->Pr, p));
+    if (pcorr) TRY(put3(h, h->PC, pcorr));
+    return TBL_OK;
+}
+
+int tbl_profile(tbl_handle* h, int enable) {
+    if (!h) return TBL_ERR_BAD_ARG;
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->prof_marks.clear();
+    h->prof_used = 0;
+    for (int q = 0; q < TBL_PROF_NGROUPS; ++q) { h->prof_ms[q] = 0; h->prof_bytes[q] = 0; h->prof_n[q] = 0; }
+    h->prof_on = enable != 0;
+    return TBL_OK;
+}
+
+int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches, int ngroups) {
+    if (!h || ngroups < 0) return TBL_ERR_BAD_ARG;
+    for (int q = 0; q < ngroups && q < TBL_PROF_NGROUPS; ++q) {
+        if (ms) ms[q] = h->prof_ms[q];
+        if (bytes) bytes[q] = h->prof_bytes[q];
+        if (launches) launches[q] = h->prof_n[q];
+    }
+    return TBL_OK;
+}
+
+static int step_loop(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
     int last = TBL_OK;
     for (int s = 0; s < nsteps; ++s) {
         last = one_step(h, stats ? &stats[s] : nullptr);
@@ -409,6 +534,25 @@ int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
             last == TBL_ERR_CUDA || last == TBL_ERR_TIMEOUT)
             return last;
     }
+    return last;
+}
+
+int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
+    if (!h || nsteps < 0) return TBL_ERR_BAD_ARG;
+    if (!h->prof_on) return step_loop(h, nsteps, stats);
+    cudaEvent_t a, b;
+    TBL_CUDA_TRY(cudaEventCreate(&a));
+    TBL_CUDA_TRY(cudaEventCreate(&b));
+    TBL_CUDA_TRY(cudaEventRecord(a, h->stream));
+    int last = step_loop(h, nsteps, stats);
+    TBL_CUDA_TRY(cudaEventRecord(b, h->stream));
+    TBL_CUDA_TRY(cudaEventSynchronize(b));
+    float ms = 0.f;
+    TBL_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+    h->prof_ms[TBL_PROF_TOTAL] += ms;
+    h->prof_n[TBL_PROF_TOTAL] += nsteps;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
     return last;
 }
 

@@ -126,6 +126,7 @@ struct tbl_handle {
     double* hpin;                  // pinned readback
     cudaStream_t stream;
     int64_t launches;
+    double npts;                   // nx*ny*nz reference points (algorithmic byte counts)
     int nstep, cont, nstat;
     double time;
     bool fluc_updated;
@@ -135,4 +136,26 @@ struct tbl_handle {
     size_t replay_pos;
     std::vector<int32_t> last_counts;
     double lamda_host;
+    // kernel-group timing (tbl_profile)
+    struct ProfMark { int group; int e0, e1; double bytes; };
+    bool prof_on;
+    std::vector<cudaEvent_t> prof_ev;
+    size_t prof_used;
+    std::vector<ProfMark> prof_marks;
+    double prof_ms[TBL_PROF_NGROUPS];
+    double prof_bytes[TBL_PROF_NGROUPS];
+    int64_t prof_n[TBL_PROF_NGROUPS];
 };
+
+namespace tbl {
+// Records a CUDA event pair around a group of launches when profiling is on.
+struct ProfScope {
+    tbl_handle* h;
+    int group;
+    double bytes;
+    int e0;
+    ProfScope(tbl_handle* h_, int g_, double b_);
+    ~ProfScope();
+};
+int prof_drain(tbl_handle* h);
+}  // namespace tbl
