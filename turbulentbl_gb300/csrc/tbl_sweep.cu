@@ -13,12 +13,12 @@
 //   * line (j,k) processes chunk c at logical step T = c + j + k, so its
 //     (j-1) and (k-1) predecessors finished chunk c at step T-1;
 //   * a warp holds 32 consecutive rows of one plane (the j-1 value comes from
-//     the neighbouring lane by shuffle); a CTA holds KG planes (the k-1 value
-//     comes through L1 after __syncthreads);
-//   * CTAs of the same slab wait for their two upstream CTAs (row block
-//     above, plane group below) through progress flags in global memory:
-//     bounded spins with acquire/release ordering; a timeout sets an error
-//     word and every CTA returns;
+//     the neighbouring lane by shuffle); a CTA holds KG planes;
+//   * every warp waits only for the warps producing its inputs: the warp of
+//     the row block above (global progress flag, acquire/release) and the
+//     warp of the plane below (shared-memory progress inside the CTA, a
+//     global flag across CTAs); waits are bounded spins, a timeout sets an
+//     error word and the warp returns;
 //   * slabs are independent (block-Jacobi GS halos come from a snapshot of the
 //     previous sweep, SSOR halos are zero), so all slabs and, for GS, all three
 //     velocity components run concurrently in one cooperative launch.
@@ -67,8 +67,36 @@ __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long 
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-constexpr long long SPIN_LIMIT = 1LL << 24;  // ~1 s with the back-off below
+constexpr long long SPIN_LIMIT = 1LL << 24;  // ~1 s of polling, then the wait gives up
 
+// Poll a global progress flag until it reports step >= target (returns the
+// step seen, or -2 on timeout).  Flags hold (epoch << 20) + step + 1.
+__device__ __forceinline__ long long wait_global(const unsigned long long* f, unsigned long long tag, long long target) {
+    long long spins = 0;
+    for (;;) {
+        unsigned long long v = ld_acquire(f);
+        long long seen = v >= tag + 1 ? (long long)(v - tag) - 1 : -1;
+        if (seen >= target) return seen;
+        if (++spins > SPIN_LIMIT) return -2;
+        if (spins > 64) __nanosleep(64);
+    }
+}
+
+// Same for a warp of this CTA through shared memory.
+__device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
+    long long spins = 0;
+    while (*p < target) {
+        if (++spins > SPIN_LIMIT) return false;
+        if (spins > 256) __nanosleep(32);
+    }
+    __threadfence_block();
+    return true;
+}
+
+// Every warp is an independent unit of the dataflow: it waits only for the
+// warps that produce its (j-1) and (k-1) inputs and publishes its own
+// progress after each step (shared memory for the next plane in the CTA,
+// a global flag for the CTAs downstream).  No CTA-wide barrier in the loop.
 template <int MODE>
 __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
     const Geom& g = a.g;
@@ -78,46 +106,48 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
     const int J = g.ny - 2, K = sl.K, C = a.C;
     const int compi = blockIdx.y;
     const int comp = MODE == SW_GS ? a.comp[compi] : 0;
-    unsigned long long* flags = a.flags + (size_t)compi * a.n_cta;
+    unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
+    __shared__ volatile int s_prog[KG];
+    if (lane == 0) s_prog[wid] = -1;
+    __syncthreads();
 
     // logical line coordinates
-    const int jl = 32 * cta.jb + lane;      // logical row
-    const int kl = KG * cta.kg + wid;       // logical plane
-    const bool line_ok = jl < J && kl < K;
+    const int jl = 32 * cta.jb + lane;  // logical row
+    const int kl = KG * cta.kg + wid;   // logical plane
+    if (kl >= K) return;                // no lines: nobody waits for this warp
+    const bool line_ok = jl < J;
     // physical coordinates (mirrored for the backward sweep)
     const int jidx = MODE == SW_BWD ? J - 1 - jl : jl;
     const int kidx = MODE == SW_BWD ? K - 1 - kl : kl;
     const int j = 1 + jidx, k = sl.bn + kidx;
-    // periodic neighbours (GS and the matvec) / plain neighbours (SSOR)
     const int jm = (j == 1) ? g.ny - 2 : j - 1;
     const int jp = (j == g.ny - 2) ? 1 : j + 1;
-    const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * (line_ok ? k : 0));
+    const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
 
-    // CTA step range
-    const int jl_last = min(32 * cta.jb + 31, J - 1), kl_last = min(KG * cta.kg + KG - 1, K - 1);
-    const int T0 = 32 * cta.jb + KG * cta.kg;
-    const int T1 = jl_last + kl_last + C - 1;
-    // upstream CTAs' last steps
-    int tend_j = -1, tend_k = -1;
-    if (cta.up_j >= 0) tend_j = (32 * cta.jb - 1) + kl_last + C - 1;  // upstream row block ends at row 32jb-1
-    if (cta.up_k >= 0) tend_k = jl_last + (KG * cta.kg - 1) + C - 1;
+    // this warp's step range and its upstream warps
+    const int jl_last = min(32 * cta.jb + 31, J - 1);
+    const int T0 = 32 * cta.jb + kl;
+    const int T1 = jl_last + kl + C - 1;
+    const int tend_k = jl_last + kl - 1 + C - 1;  // last step of the (k-1) upstream warp
+    const unsigned long long* fj = cta.up_j >= 0 ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
+    const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
+    unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
+    const unsigned long long tag = a.epoch << 20;
 
     // per-plane coefficients
-    double cW = 0, cE = 0, cS = 0, cN = 0, cB = 0, cT = 0, rd = 0, wr = 0, sk = 0;
-    if (line_ok) {
-        if (MODE == SW_GS) {
-            cE = a.t * a.aw; cW = cE; cN = a.t * a.as; cS = cN;
-            cT = a.t * a.At[k]; cB = a.t * a.Ab[k];
-            rd = 1.0 / (1.0 + (a.t * a.Ap[k]));
-        } else {
-            wr = -a.omega * a.rAp[k];           // -w * rAnp
-            sk = a.sw * a.Ap[k];                 // ((2-w)/w) * Anp
-        }
+    double cW = 0, cE = 0, cS = 0, cN = 0, cB = 0, cT = 0, rd = 0, wr = 0, sk = 0, ab = 0, at = 0, ap = 0;
+    if (MODE == SW_GS) {
+        cE = a.t * a.aw; cW = cE; cN = a.t * a.as; cS = cN;
+        cT = a.t * a.At[k]; cB = a.t * a.Ab[k];
+        rd = 1.0 / (1.0 + (a.t * a.Ap[k]));
+    } else {
+        wr = -a.omega * a.rAp[k];  // -w * rAnp
+        sk = a.sw * a.Ap[k];       // ((2-w)/w) * Anp
+        ab = a.Ab[k]; at = a.At[k]; ap = a.Ap[k];
     }
     double* F = MODE == SW_GS ? a.F[comp] : nullptr;
     const double* Qc = MODE == SW_GS ? a.Q[comp] : nullptr;
     const size_t hplane = (size_t)g.ps;
-    // halo planes for GS: lo (below bn) and hi (above bn+K-1) of this slab
     const double* halo_lo = nullptr;
     const double* halo_hi = nullptr;
     if (MODE == SW_GS) {
@@ -130,13 +160,10 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
     double carry = 0.0;  // logical previous point on the own line
 #pragma unroll
     for (int e = 0; e < CHUNK; ++e) last[e] = 0.0;
-
-    __shared__ int s_abort;
-    if (threadIdx.x == 0) s_abort = 0;
-    __syncthreads();
+    long long seen_j = -1, seen_k = -1;  // upstream progress known to lane 0
 
     for (int T = T0; T <= T1; ++T) {
-        const int cl = T - jl - kl;  // logical chunk
+        const int cl = T - jl - kl;  // logical chunk of this lane
         const bool act = line_ok && cl >= 0 && cl < C;
         const int c = MODE == SW_BWD ? C - 1 - cl : cl;  // physical chunk
         const int i0 = 4 * c;
@@ -150,7 +177,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
 #pragma unroll
                 for (int e = 0; e < CHUNK; ++e) { oi[e] = Fl[e]; rhs[e] = Ql[e]; }
                 if (i0 + 3 <= g.nx - 2) nxt = Fl[4];
-                if (jp != 1) {  // the wrapped row (new values) is read after the wait
+                if (jp != 1) {  // the wrapped row holds new values: read after the wait
                     const double* Fj = F + (long long)g.sx * ((long long)jp + (long long)g.ny * k) + i0;
 #pragma unroll
                     for (int e = 0; e < CHUNK; ++e) ojp[e] = __ldcg(Fj + e);
@@ -166,7 +193,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
                 const double* Xjp = a.X + (long long)g.sx * ((long long)jp + (long long)g.ny * k) + i0;
                 const double* Xkm = Xl - g.ps;
                 const double* Xkp = Xl + g.ps;
-                const double ab = a.Ab[k], at = a.At[k], ap = a.Ap[k];
 #pragma unroll
                 for (int e = 0; e < CHUNK; ++e) {
                     const int i = i0 + e;
@@ -183,26 +209,30 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
                 for (int e = 0; e < CHUNK; ++e) rhs[e] = sk * Rl[e];
             }
         }
-        // ---- wait for the upstream CTAs to finish step T-1
-        if (threadIdx.x == 0) {
-            long long spins = 0;
-            if (cta.up_j >= 0 && T - 1 >= 0) {
-                const unsigned long long target = (a.epoch << 20) + (unsigned long long)(min(T - 1, tend_j) + 1);
-                while (ld_acquire(&flags[cta.up_j]) < target) {
-                    if (++spins > SPIN_LIMIT) { s_abort = 1; atomicExch(a.err, TBL_ERR_TIMEOUT); break; }
-                    __nanosleep(32);
+        // ---- wait for the producers of step T-1 (lane 0 polls for the warp)
+        const int cl0 = T - 32 * cta.jb - kl;           // lane 0's chunk
+        const bool lane0_act = cl0 >= 0 && cl0 < C;
+        const bool any_act = cl0 >= 0 && (T - jl_last - kl) < C;
+        int abort = 0;
+        if (lane == 0 && any_act) {
+            if (fj && lane0_act && seen_j < T - 1) {
+                seen_j = wait_global(fj, tag, T - 1);
+                if (seen_j < 0) abort = 1;
+            }
+            if (!abort && kl > 0) {
+                const int target = min(T - 1, tend_k);
+                if (wid > 0) {
+                    if (!wait_shared(&s_prog[wid - 1], target)) abort = 1;
+                } else if (fk && seen_k < target) {
+                    seen_k = wait_global(fk, tag, target);
+                    if (seen_k < 0) abort = 1;
                 }
             }
-            if (!s_abort && cta.up_k >= 0 && T - 1 >= 0) {
-                const unsigned long long target = (a.epoch << 20) + (unsigned long long)(min(T - 1, tend_k) + 1);
-                while (ld_acquire(&flags[cta.up_k]) < target) {
-                    if (++spins > SPIN_LIMIT) { s_abort = 1; atomicExch(a.err, TBL_ERR_TIMEOUT); break; }
-                    __nanosleep(32);
-                }
-            }
+            if (abort) atomicExch(a.err, TBL_ERR_TIMEOUT);
         }
-        __syncthreads();
-        if (s_abort) return;
+        abort = __shfl_sync(0xffffffffu, abort, 0);
+        if (abort) return;
+        __syncwarp();
         // ---- predecessor values: (j-1) by shuffle or global, (k-1) through memory
         double pj[CHUNK], pk[CHUNK];
 #pragma unroll
@@ -285,7 +315,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
                 for (int e = 0; e < CHUNK; ++e) {
                     const int i = i0 + e;
                     if (i >= 1 && i <= g.nx - 2) {
-                        double x = (rhs[e] + a.aw * prev + a.as * pj[e] + a.Ab[k] * pk[e]) * wr;
+                        double x = (rhs[e] + a.aw * prev + a.as * pj[e] + ab * pk[e]) * wr;
                         nv[e] = x;
                         prev = x;
                     } else {
@@ -303,7 +333,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
                 for (int e = CHUNK - 1; e >= 0; --e) {
                     const int i = i0 + e;
                     if (i >= 1 && i <= g.nx - 2) {
-                        double y = (rhs[e] + a.aw * prev + a.as * pj[e] + a.At[k] * pk[e]) * wr;
+                        double y = (rhs[e] + a.aw * prev + a.as * pj[e] + at * pk[e]) * wr;
                         nv[e] = y;
                         prev = y;
                     } else {
@@ -319,11 +349,12 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
 #pragma unroll
             for (int e = 0; e < CHUNK; ++e) last[e] = nv[e];
         }
-        // ---- publish step T
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            st_release(&flags[blockIdx.x], (a.epoch << 20) + (unsigned long long)(T + 1));
+        // ---- publish step T: the next plane of this CTA, then the CTAs downstream
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            s_prog[wid] = T;
+            st_release(fme, tag + (unsigned long long)(T + 1));
         }
     }
 }
@@ -355,8 +386,8 @@ int build_sweep_ctas(tbl_handle* h) {
     TBL_CUDA_TRY(cudaMemcpy(h->ctas, ctas.data(), ctas.size() * sizeof(SweepCta), cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMalloc(&h->slabs, slabs.size() * sizeof(SlabDesc)));
     TBL_CUDA_TRY(cudaMemcpy(h->slabs, slabs.data(), slabs.size() * sizeof(SlabDesc), cudaMemcpyHostToDevice));
-    TBL_CUDA_TRY(cudaMalloc(&h->flags, (size_t)3 * h->n_cta * sizeof(unsigned long long)));
-    TBL_CUDA_TRY(cudaMemset(h->flags, 0, (size_t)3 * h->n_cta * sizeof(unsigned long long)));
+    TBL_CUDA_TRY(cudaMalloc(&h->flags, (size_t)3 * h->n_cta * KG * sizeof(unsigned long long)));
+    TBL_CUDA_TRY(cudaMemset(h->flags, 0, (size_t)3 * h->n_cta * KG * sizeof(unsigned long long)));
     h->epoch = 1;
     return TBL_OK;
 }
