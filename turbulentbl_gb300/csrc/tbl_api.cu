@@ -75,6 +75,28 @@ static int get3(tbl_handle* h, double* dst, const double* src) {
     return TBL_OK;
 }
 
+// FP32 fields: converted on the host through a staging buffer
+static int put3f(tbl_handle* h, float* dst, const double* src) {
+    const Geom& g = h->g;
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    std::vector<float> tmp(n);
+    for (size_t q = 0; q < n; ++q) tmp[q] = (float)src[q];
+    TBL_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)g.sx * 4, tmp.data(), (size_t)g.nx * 4, (size_t)g.nx * 4,
+                                   (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return TBL_OK;
+}
+static int get3f(tbl_handle* h, double* dst, const float* src) {
+    const Geom& g = h->g;
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    std::vector<float> tmp(n);
+    TBL_CUDA_TRY(cudaMemcpy2DAsync(tmp.data(), (size_t)g.nx * 4, src, (size_t)g.sx * 4, (size_t)g.nx * 4,
+                                   (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (size_t q = 0; q < n; ++q) dst[q] = (double)tmp[q];
+    return TBL_OK;
+}
+
 template <typename T>
 static int dalloc(T** p, size_t n) {
     TBL_CUDA_TRY(cudaMalloc((void**)p, n * sizeof(T)));
@@ -89,6 +111,10 @@ static int dalloc(T** p, size_t n) {
     } while (0)
 
 static void free_all(tbl_handle* h) {
+    void* mptrs[] = {h->Uf[0], h->Uf[1], h->Uf[2], h->Pf, h->Qf[0], h->Qf[1], h->Qf[2], h->Df[0], h->Df[1],
+                     h->Df[2], h->Vf, h->RHf, h->R64};
+    for (void* p : mptrs)
+        if (p) cudaFree(p);
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
                     h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->usum2, h->vsum2,
                     h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
@@ -106,7 +132,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
     Geom& g = h->g;
     g.nx = nx; g.ny = ny; g.nz = nz;
-    g.sx = ((nx + 2) + 7) / 8 * 8;
+    g.sx = ((nx + 7) + 7) / 8 * 8;  // a 32-byte chunk starting at i <= nx-2 stays inside the row
     g.ps = (long long)g.sx * ny;
     g.vol = g.ps * nz;
     g.J = ny - 2;
@@ -123,9 +149,22 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TBL_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     TBL_CUDA_TRY(cudaMallocHost(&h->hpin, 4096));
     const size_t vol = (size_t)g.vol, n2 = (size_t)nx * nz, pl = (size_t)ny * nz;
-    for (int c = 0; c < 3; ++c) { TRY(dalloc(&h->U[c], vol)); TRY(dalloc(&h->Q[c], vol)); }
-    TRY(dalloc(&h->Pr, vol)); TRY(dalloc(&h->PC, vol)); TRY(dalloc(&h->Q8, vol)); TRY(dalloc(&h->RH, vol));
-    TRY(dalloc(&h->V, vol * (size_t)(cfg->kmax + 1)));
+    TRY(dalloc(&h->PC, vol));
+    TRY(dalloc(&h->Q8, vol));
+    if (cfg->precision == TBL_PREC_MIXED) {
+        for (int c = 0; c < 3; ++c) {
+            TRY(dalloc(&h->Uf[c], vol));
+            TRY(dalloc(&h->Qf[c], vol));
+            TRY(dalloc(&h->Df[c], vol));
+        }
+        TRY(dalloc(&h->Pf, vol));
+        TRY(dalloc(&h->RHf, vol));
+        TRY(dalloc(&h->Vf, vol * (size_t)(cfg->mixed_kmax + 1)));
+    } else {
+        for (int c = 0; c < 3; ++c) { TRY(dalloc(&h->U[c], vol)); TRY(dalloc(&h->Q[c], vol)); }
+        TRY(dalloc(&h->Pr, vol)); TRY(dalloc(&h->RH, vol));
+        TRY(dalloc(&h->V, vol * (size_t)(cfg->kmax + 1)));
+    }
     TRY(dalloc(&h->uold1, pl));
     TRY(dalloc(&h->x3, (size_t)nz)); TRY(dalloc(&h->jacinv, (size_t)nz)); TRY(dalloc(&h->jac2, (size_t)nz));
     TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
@@ -137,7 +176,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->sums, 9 * n2)); TRY(dalloc(&h->bl_out, 4 * (size_t)nx));
     TRY(dalloc(&h->slab_of_k, (size_t)nz));
     TRY(dalloc(&h->sc, 1));
-    const int K1 = cfg->kmax + 1;
+    const int K1 = (cfg->precision == TBL_PREC_MIXED ? cfg->mixed_kmax : cfg->kmax) + 1;
     TRY(dalloc(&h->h, (size_t)K1 * K1)); TRY(dalloc(&h->gg, (size_t)K1)); TRY(dalloc(&h->gc, (size_t)K1));
     TRY(dalloc(&h->gs, (size_t)K1)); TRY(dalloc(&h->gy, (size_t)K1));
     h->red.max_blocks = 2048;
@@ -192,6 +231,9 @@ static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
     int sweeps[3] = {0, 0, 0};
     double sumnor[3] = {0, 0, 0}, sumav[3] = {0, 0, 0};
     int parity = 0;
+    const bool mixed = h->cfg.precision == TBL_PREC_MIXED;
+    if (mixed)
+        for (int c = 0; c < 3; ++c) TRY(launch_gs_delta_init(h, c));
     TRY(launch_halo_init(h, parity));
     const int nb = red_blocks(h);
     for (int it = 1; it <= mmax; ++it) {
@@ -226,7 +268,100 @@ static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
         for (int q = 0; q < n; ++q) sweeps[comps[q]]++;
     }
     for (int c = 0; c < 3; ++c) { st.gs_sweeps[c] = sweeps[c]; st.gs_resid[c] = sumav[c]; }
+    if (mixed)
+        for (int c = 0; c < 3; ++c) TRY(launch_gs_delta_apply(h, c));
     return TBL_OK;
+}
+
+// ---------------------------------------------- mixed-precision Poisson solve
+// FP64 iterative refinement around FP32 GMRES(mixed_kmax): every outer pass
+// forms r = Q8 - L7 p' in FP64, runs one FP32 Arnoldi cycle with the FP32
+// block-SSOR preconditioner (FP64 Gram-Schmidt sums, Hessenberg and Givens),
+// and adds the correction to the FP64 p'.  Stops when the preconditioned
+// residual relative to the first pass is <= mixed_outer_tol; an inner cycle
+// stops at mixed_kmax, at mixed_inner_tol relative to its own start, or at the
+// outer tolerance.
+static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats& st) {
+    const int kmax = h->cfg.mixed_kmax, K1 = kmax + 1;
+    const size_t vol = (size_t)h->g.vol;
+    const double outer_tol = h->cfg.mixed_outer_tol, inner_tol = h->cfg.mixed_inner_tol;
+    double sumav = 1.0, sumnor = 0.0;
+    int m = 0, iters = 0;
+    int status = TBL_OK;
+    const double wN = 4.0 * h->npts;
+    while (sumav > outer_tol && m < h->cfg.mixed_max_outer) {
+        m = m + 1;
+        float* V0 = h->Vf;
+        {
+            ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN + 2.0 * 8.0 * h->npts);
+            TRY(launch_ssor_fwd_f(h, nullptr, h->PC, h->Q8));
+        }
+        {
+            ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
+            TRY(launch_ssor_bwd_f(h, V0));
+        }
+        {
+            ProfScope ps(h, TBL_PROF_MGS, 1.0 * wN);
+            TRY(launch_dot_f(h, V0, V0, &h->sc->rho, 1));
+        }
+        TRY(launch_restart_init_k(h, m == 1, K1));
+        TRY(readback(h, &h->sc->rho, 4 * sizeof(double)));
+        const double rho_m = h->hpin[0];
+        if (m == 1) {
+            if (!(rho_m > 0.0)) { status = TBL_ERR_ZERO_RHS; break; }
+            sumnor = rho_m;
+        }
+        sumav = h->hpin[2];
+        if (sumav <= outer_tol) { kits.push_back(0); break; }
+        {
+            ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
+            TRY(launch_scale_by_inv_f(h, V0, &h->sc->rho));
+        }
+        int kit = 0;
+        while (kit < kmax && sumav > outer_tol && sumav * sumnor > inner_tol * rho_m) {
+            kit = kit + 1;
+            float* W = h->Vf + (size_t)kit * vol;
+            {
+                ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN);
+                TRY(launch_ssor_fwd_f(h, h->Vf + (size_t)(kit - 1) * vol, nullptr, nullptr));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
+                TRY(launch_ssor_bwd_f(h, W));
+            }
+            double* hcol = h->h + (size_t)K1 * (kit - 1);
+            {
+                ProfScope ps(h, TBL_PROF_MGS, (2.0 + 4.0 * (kit - 1) + 3.0) * wN);
+                TRY(launch_mgs_f(h, W, nullptr, nullptr, V0, &hcol[0], 0));
+                for (int kk = 1; kk <= kit - 1; ++kk)
+                    TRY(launch_mgs_f(h, W, h->Vf + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->Vf + (size_t)kk * vol,
+                                     &hcol[kk], 0));
+                TRY(launch_mgs_f(h, W, h->Vf + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_SMALL, 0.0);
+                TRY(launch_givens_k(h, kit, K1));
+            }
+            {
+                ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
+                TRY(launch_scale_by_inv_f(h, W, &h->sc->red[8]));
+            }
+            TRY(readback(h, &h->sc->sumav, sizeof(double)));
+            sumav = h->hpin[0];
+        }
+        iters += kit;
+        kits.push_back(kit);
+        if (kit > 0) {
+            ProfScope ps(h, TBL_PROF_VEC, (kit * 4.0 + 16.0) * h->npts);
+            TRY(launch_backsub_update_f(h, kit));
+        }
+    }
+    st.gmres_restarts = m;
+    st.outer_iters = m;
+    st.gmres_iters = iters;
+    st.gmres_resid = sumav;
+    if (status == TBL_OK && sumav > outer_tol) status = TBL_ERR_NOT_CONVERGED;
+    return status;
 }
 
 // ------------------------------------------------------------ GMRES
@@ -345,7 +480,7 @@ static int one_step(tbl_handle* h, tbl_step_stats* out) {
         TRY(launch_pc_zero_faces(h));
     }
     std::vector<int32_t> kits;
-    int status = gmres(h, rec, kits, st);
+    int status = c.precision == TBL_PREC_MIXED ? gmres_mixed(h, kits, st) : gmres(h, rec, kits, st);
     if (status == TBL_ERR_ZERO_RHS || status < 0 && status != TBL_ERR_NOT_CONVERGED) return status;
     if (c.flags & TBL_FLAG_PPE_RESIDUAL) {
         TRY(launch_ppe_resid(h));
@@ -422,6 +557,10 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
     if (cfg->irec < 2 || cfg->irec > cfg->nx - 1 || cfg->cum < 1 || cfg->istat < 1) return TBL_ERR_BAD_ARG;
     if (cfg->kmax < 1 || cfg->mmax < 1 || !(cfg->dt > 0) || !(cfg->re > 0)) return TBL_ERR_BAD_ARG;
     if (cfg->precision != TBL_PREC_FP64 && cfg->precision != TBL_PREC_MIXED) return TBL_ERR_BAD_ARG;
+    if (cfg->precision == TBL_PREC_MIXED &&
+        (cfg->mixed_kmax < 1 || cfg->mixed_max_outer < 1 || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
+        return TBL_ERR_BAD_ARG;
+    if (cfg->precision == TBL_PREC_MIXED && (cfg->flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TBL_ERR_NO_DEVICE;
     tbl_handle* h = new (std::nothrow) tbl_handle();
@@ -446,10 +585,17 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
     for (int k = 0; k < c.nz; ++k)
         if (st->newk[k] < 1 || st->newk[k] > c.nz) return TBL_ERR_BAD_ARG;
     const size_t n2 = (size_t)c.nx * c.nz, pl = (size_t)c.ny * c.nz;
-    TRY(put3(h, h->U[0], st->u));
-    TRY(put3(h, h->U[1], st->v));
-    TRY(put3(h, h->U[2], st->w));
-    TRY(put3(h, h->Pr, st->p));
+    if (c.precision == TBL_PREC_MIXED) {
+        TRY(put3f(h, h->Uf[0], st->u));
+        TRY(put3f(h, h->Uf[1], st->v));
+        TRY(put3f(h, h->Uf[2], st->w));
+        TRY(put3f(h, h->Pf, st->p));
+    } else {
+        TRY(put3(h, h->U[0], st->u));
+        TRY(put3(h, h->U[1], st->v));
+        TRY(put3(h, h->U[2], st->w));
+        TRY(put3(h, h->Pr, st->p));
+    }
     if (st->pcorr) TRY(put3(h, h->PC, st->pcorr));
     else TBL_CUDA_TRY(cudaMemsetAsync(h->PC, 0, (size_t)h->g.vol * 8, h->stream));
     TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2, st->usum2, n2 * 8, cudaMemcpyHostToDevice, h->stream));
@@ -498,10 +644,17 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
 int tbl_upload_fields(tbl_handle* h, const double* u, const double* v, const double* w, const double* p,
                       const double* pcorr) {
     if (!h || !u || !v || !w || !p) return TBL_ERR_BAD_ARG;
-    TRY(put3(h, h->U[0], u));
-    TRY(put3(h, h->U[1], v));
-    TRY(put3(h, h->U[2], w));
-    TRY(put3(h, h->Pr, p));
+    if (h->cfg.precision == TBL_PREC_MIXED) {
+        TRY(put3f(h, h->Uf[0], u));
+        TRY(put3f(h, h->Uf[1], v));
+        TRY(put3f(h, h->Uf[2], w));
+        TRY(put3f(h, h->Pf, p));
+    } else {
+        TRY(put3(h, h->U[0], u));
+        TRY(put3(h, h->U[1], v));
+        TRY(put3(h, h->U[2], w));
+        TRY(put3(h, h->Pr, p));
+    }
     if (pcorr) TRY(put3(h, h->PC, pcorr));
     return TBL_OK;
 }
@@ -560,10 +713,11 @@ int tbl_download_state(tbl_handle* h, tbl_state* st) {
     if (!h || !st) return TBL_ERR_BAD_ARG;
     const tbl_config& c = h->cfg;
     const size_t n2 = (size_t)c.nx * c.nz, pl = (size_t)c.ny * c.nz, N = (size_t)c.nx * c.ny * c.nz;
-    if (st->u) TRY(get3(h, st->u, h->U[0]));
-    if (st->v) TRY(get3(h, st->v, h->U[1]));
-    if (st->w) TRY(get3(h, st->w, h->U[2]));
-    if (st->p) TRY(get3(h, st->p, h->Pr));
+    const bool mx = c.precision == TBL_PREC_MIXED;
+    if (st->u) TRY(mx ? get3f(h, st->u, h->Uf[0]) : get3(h, st->u, h->U[0]));
+    if (st->v) TRY(mx ? get3f(h, st->v, h->Uf[1]) : get3(h, st->v, h->U[1]));
+    if (st->w) TRY(mx ? get3f(h, st->w, h->Uf[2]) : get3(h, st->w, h->U[2]));
+    if (st->p) TRY(mx ? get3f(h, st->p, h->Pf) : get3(h, st->p, h->Pr));
     if (st->pcorr) TRY(get3(h, st->pcorr, h->PC));
     if (st->usum2) TBL_CUDA_TRY(cudaMemcpyAsync(st->usum2, h->usum2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
     if (st->vsum2) TBL_CUDA_TRY(cudaMemcpyAsync(st->vsum2, h->vsum2, n2 * 8, cudaMemcpyDeviceToHost, h->stream));
@@ -585,7 +739,7 @@ int tbl_download_state(tbl_handle* h, tbl_state* st) {
         for (int cc = 0; cc < 3; ++cc) {
             if (!uf[cc]) continue;
             TRY(get3(h, uf[cc], h->ufl_full + (size_t)cc * h->g.vol));
-            TRY(get3(h, U.data(), h->U[cc]));
+            TRY(mx ? get3f(h, U.data(), h->Uf[cc]) : get3(h, U.data(), h->U[cc]));
             TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
             if (h->fluc_updated)
                 for (int k = 1; k <= c.nz - 2; ++k)

@@ -1,8 +1,9 @@
 // tbl_internal.cuh -- device state and kernel interfaces of libtblgpu.so.
 //
 // Layout in HBM: every 3-D field is the reference array Ut(nx,ny,nz,.) with
-// i fastest, stored with a row pitch sx = nx rounded up to 8 elements so that
-// each row starts on a 64-byte boundary (32-byte FP64 chunks stay aligned).
+// i fastest, stored with a row pitch sx = nx+7 rounded up to 8 elements so
+// that each row starts on a 32-byte boundary and a 32-byte chunk of a
+// wavefront lane never crosses a row.
 // Element (i,j,k) (0-based) is at i + sx*(j + ny*k).  Padding columns hold 0.
 #pragma once
 #include <cuda_runtime.h>
@@ -94,6 +95,14 @@ struct tbl_handle {
     double* RH;      // SSOR forward result (scaled)
     double* V;       // kmax+1 Krylov vectors, vol each
     double* uold1;   // U1 at i=1 before the inflow update, (ny, nz)
+    // mixed precision (TBL_PREC_MIXED): FP32 fields and inner-GMRES vectors
+    float* Uf[3];
+    float* Pf;
+    float* Qf[3];
+    float* Df[3];    // GS increments (delta form)
+    float* Vf;       // inner Krylov vectors
+    float* RHf;      // inner SSOR work
+    double* R64;     // FP64 outer residual
     // per-k coefficient arrays and mesh (nz)
     double *x3, *jacinv, *jac2, *Ab, *At, *Ap, *rAp;
     // recycling state

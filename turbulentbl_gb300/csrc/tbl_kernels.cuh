@@ -16,6 +16,8 @@ int launch_div_diag(tbl_handle* h, int nblocks, int slot);
 int launch_fluc_ke(tbl_handle* h, int nblocks, int slot);
 int launch_stats(tbl_handle* h);
 int launch_rescale(tbl_handle* h);
+int launch_gs_delta_init(tbl_handle* h, int comp);
+int launch_gs_delta_apply(tbl_handle* h, int comp);
 
 // tbl_sweep.cu
 int build_sweep_ctas(tbl_handle* h);
@@ -24,6 +26,8 @@ int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity);
 int launch_halo_init(tbl_handle* h, int parity);
 int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8);
 int launch_ssor_bwd(tbl_handle* h, double* out);
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8);
+int launch_ssor_bwd_f(tbl_handle* h, float* out);
 
 // tbl_krylov.cu
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);
@@ -34,5 +38,11 @@ int launch_backsub_update(tbl_handle* h, int kit);
 int launch_restart_init(tbl_handle* h, int first);
 int launch_ppe_resid(tbl_handle* h);
 int red_blocks(tbl_handle* h);
+int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int op);
+int launch_mgs_f(tbl_handle* h, float* w, const float* vk, const double* hk, const float* vn, double* out, int op);
+int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom);
+int launch_backsub_update_f(tbl_handle* h, int kit);
+int launch_restart_init_k(tbl_handle* h, int first, int K1);
+int launch_givens_k(tbl_handle* h, int kit, int K1);
 
 }  // namespace tbl

@@ -178,6 +178,74 @@ __global__ void __launch_bounds__(RED_THREADS) k_ppe_resid(Geom g, double aw, do
     grid_finish(b2, rw, 10, gridDim.x, blockIdx.x, &sc->red[10], 0);
 }
 
+// ------------------------------------------------ mixed precision (FP32)
+// Inner GMRES vectors are FP32; dot products accumulate in FP64 (the FP32
+// products of 4 consecutive elements are summed in FP32, then added in FP64),
+// and h, g, c, s, y stay FP64 (k_restart_init / k_givens / k_backsub above).
+
+__device__ __forceinline__ double dot4(float4 a, float4 b) {
+    return (double)fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_dot_f(long long n4, const float4* __restrict__ a,
+                                                       const float4* __restrict__ b, RedWork rw, int slot,
+                                                       double* out, int op) {
+    __shared__ double s_red[RED_THREADS / 32];
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x)
+        acc += dot4(a[q], b[q]);
+    double bt = block_sum(acc, s_red);
+    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_mgs_f(long long n4, float4* __restrict__ w,
+                                                       const float4* __restrict__ vk, const double* __restrict__ hk,
+                                                       const float4* __restrict__ vn, RedWork rw, int slot,
+                                                       double* out, int op) {
+    __shared__ double s_red[RED_THREADS / 32];
+    const float hv = vk ? (float)*hk : 0.0f;
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+        float4 x = w[q];
+        if (vk) {
+            float4 v = vk[q];
+            x.x = fmaf(-hv, v.x, x.x);
+            x.y = fmaf(-hv, v.y, x.y);
+            x.z = fmaf(-hv, v.z, x.z);
+            x.w = fmaf(-hv, v.w, x.w);
+            w[q] = x;
+        }
+        acc += dot4(vn ? vn[q] : x, x);
+    }
+    double bt = block_sum(acc, s_red);
+    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
+}
+
+__global__ void k_scale_inv_f(long long n4, float4* __restrict__ w, const double* __restrict__ denom) {
+    const double d = *denom;
+    if (!(d > 0.0 || d < 0.0)) return;
+    const float r = (float)(1.0 / d);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+        float4 x = w[q];
+        x.x *= r; x.y *= r; x.z *= r; x.w *= r;
+        w[q] = x;
+    }
+}
+
+// p' (FP64) += sum_i y_i v_i (FP32 vectors), accumulated in FP64
+__global__ void k_update_f(long long n4, double* __restrict__ pc, const float4* __restrict__ V, long long vstride4,
+                           const double* __restrict__ gy, int kit) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+        double4 x = reinterpret_cast<double4*>(pc)[q];
+        for (int i = 0; i < kit; ++i) {
+            float4 v = V[(long long)i * vstride4 + q];
+            double y = gy[i];
+            x.x += (double)v.x * y; x.y += (double)v.y * y; x.z += (double)v.z * y; x.w += (double)v.w * y;
+        }
+        reinterpret_cast<double4*>(pc)[q] = x;
+    }
+}
+
 // ------------------------------------------------------------- host glue
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op) {
     int nb = red_blocks(h);
@@ -222,6 +290,50 @@ int launch_backsub_update(tbl_handle* h, int kit) {
     k_update<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)h->PC, (const double2*)h->V, h->g.vol / 2,
                                                 h->gy, kit);
     h->launches += 2;
+    return TBL_OK;
+}
+
+int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int op) {
+    int nb = red_blocks(h);
+    k_dot_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (const float4*)a, (const float4*)b, h->red, 7, out, op);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_mgs_f(tbl_handle* h, float* w, const float* vk, const double* hk, const float* vn, double* out, int op) {
+    int nb = red_blocks(h);
+    k_mgs_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (float4*)w, (const float4*)vk, hk, (const float4*)vn,
+                                               h->red, 7, out, op);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom) {
+    int nb = red_blocks(h);
+    k_scale_inv_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (float4*)w, denom);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_backsub_update_f(tbl_handle* h, int kit) {
+    const int K1 = h->cfg.mixed_kmax + 1;
+    k_backsub<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gy);
+    int nb = red_blocks(h);
+    k_update_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, h->PC, (const float4*)h->Vf, h->g.vol / 4, h->gy,
+                                                  kit);
+    h->launches += 2;
+    return TBL_OK;
+}
+
+int launch_restart_init_k(tbl_handle* h, int first, int K1) {
+    k_restart_init<<<1, 256, 0, h->stream>>>(K1, h->h, h->gg, h->gc, h->gs, h->gy, h->sc, first);
+    h->launches++;
+    return TBL_OK;
+}
+
+int launch_givens_k(tbl_handle* h, int kit, int K1) {
+    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc);
+    h->launches++;
     return TBL_OK;
 }
 

@@ -23,7 +23,8 @@ __device__ __forceinline__ int jp2(const Geom& g, int j) { return j == g.ny - 3 
 
 // ------------------------------------------------------------------ inflow
 // Utold(1,:,:,1) = Ut(1,:,:,1) (dnstbl2/dnstbl.f90:549; only this plane is read later)
-__global__ void k_save_uold(Geom g, const double* __restrict__ u1, double* __restrict__ uold1) {
+template <typename T>
+__global__ void k_save_uold(Geom g, const T* __restrict__ u1, double* __restrict__ uold1) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.ny * g.nz) return;
     int j = t % g.ny, k = t / g.ny;
@@ -31,7 +32,8 @@ __global__ void k_save_uold(Geom g, const double* __restrict__ u1, double* __res
 }
 
 // Recycling inflow (dnstbl2/dnstbl.f90:557-618).  One thread per (j,k).
-__global__ void k_inflow(Geom g, double* __restrict__ u1, double* __restrict__ u2, double* __restrict__ u3,
+template <typename T>
+__global__ void k_inflow(Geom g, T* __restrict__ u1, T* __restrict__ u2, T* __restrict__ u3,
                          const double* __restrict__ usum2, const double* __restrict__ vsum2,
                          const double* __restrict__ wsum2, const double* __restrict__ wt,
                          const double* __restrict__ ume1, const int* __restrict__ newk,
@@ -58,78 +60,83 @@ __global__ void k_inflow(Geom g, double* __restrict__ u1, double* __restrict__ u
         double lam = sc->lamda;
         double f1 = lam * src[pj], f2 = lam * src[pl + pj], f3 = lam * src[2 * pl + pj];
         double w_ = wt[(size_t)(nx - 2) + (size_t)nx * k];  // Wt(nX-1,k): the redundant i loop (:594-600)
-        u1[q] = (uin + f1) * (1.0 - w_) + (uin + f1) * w_;
-        u2[q] = (vin + f2) * (1.0 - w_) + (vin + f2) * w_;
-        u3[q] = (win + f3) * (1.0 - w_) + (win + f3) * w_;
+        u1[q] = (T)((uin + f1) * (1.0 - w_) + (uin + f1) * w_);
+        u2[q] = (T)((vin + f2) * (1.0 - w_) + (vin + f2) * w_);
+        u3[q] = (T)((win + f3) * (1.0 - w_) + (win + f3) * w_);
     } else {
-        u1[q] = usum2[ir];
-        u2[q] = vsum2[ir];
-        u3[q] = wsum2[ir];
+        u1[q] = (T)usum2[ir];
+        u2[q] = (T)vsum2[ir];
+        u3[q] = (T)wsum2[ir];
     }
 }
 
 // ------------------------------------------------------- convection + RHS
+template <typename R>
 struct ConvCoef {
-    double tf, dx, dy, invdx, invdy, invdxi;
-    double inv2dx;    // 1/(2 dx)
-    double c12x, c12y, c12z;  // onetwelfth*inv
-    double q25x, q25y, q25z;  // 0.25*inv
-    double h05z;      // 0.5*invdxi
-    double dt;
+    R tf, dx, dy, invdx, invdy, invdxi;
+    R inv2dx;    // 1/(2 dx)
+    R c12x, c12y, c12z;  // onetwelfth*inv
+    R q25x, q25y, q25z;  // 0.25*inv
+    R h05z;      // 0.5*invdxi
+    R dt;
 };
 
 // Convection of F along x (dnstbl2/dnstbl.f90:651-664)
-__device__ __forceinline__ double conv_x(double u, bool nearb, double fm2, double fm1, double f0, double fp1,
-                                         double fp2, const ConvCoef& c) {
-    double sgn = u > -1.0 ? 1.0 : -1.0;  // sign(1, ceiling(u))
-    double Pe = sgn * c.tf * u * c.dx;
+template <typename R>
+__device__ __forceinline__ R conv_x(R u, bool nearb, R fm2, R fm1, R f0, R fp1, R fp2,
+                                    const ConvCoef<R>& c) {
+    R sgn = u > R(-1) ? R(1) : R(-1);  // sign(1, ceiling(u))
+    R Pe = sgn * c.tf * u * c.dx;
     if (nearb) return u * (fp1 - fm1) * c.inv2dx;
-    if (Pe > 2.0 && Pe < 50.0) {
-        double t1 = fabs(u) * (fp2 - 4.0 * fp1 + 6.0 * f0 - 4.0 * fm1 + fm2) * c.q25x;
-        double t2 = u * (-fp2 + 8.0 * fp1 - 8.0 * fm1 + fm2) * c.c12x;
+    if (Pe > R(2) && Pe < R(50)) {
+        R t1 = abs(u) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25x;
+        R t2 = u * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12x;
         return t1 + t2;
     }
-    return u * ((fm2 - 8.0 * fm1 + 8.0 * fp1 - fp2) * c.c12x);
+    return u * ((fm2 - R(8) * fm1 + R(8) * fp1 - fp2) * c.c12x);
 }
 
 // y: first-order upwind at the first/last unique rows (:670-677)
-__device__ __forceinline__ double conv_y(double v, bool nearb, double fm2, double fm1, double f0, double fp1,
-                                         double fp2, const ConvCoef& c) {
-    double sgn = v > -1.0 ? 1.0 : -1.0;
-    double Pe = sgn * c.tf * v * c.dy;
+template <typename R>
+__device__ __forceinline__ R conv_y(R v, bool nearb, R fm2, R fm1, R f0, R fp1, R fp2,
+                                    const ConvCoef<R>& c) {
+    R sgn = v > R(-1) ? R(1) : R(-1);
+    R Pe = sgn * c.tf * v * c.dy;
     if (nearb) {
-        double a1 = fmax(v, 0.0), b = fmin(v, 0.0);
+        R a1 = max(v, R(0)), b = min(v, R(0));
         return a1 * ((f0 - fm1) * c.invdy) + b * ((fp1 - f0) * c.invdy);
     }
-    if (Pe > 2.0 && Pe < 50.0) {
-        double t1 = fabs(v) * (fp2 - 4.0 * fp1 + 6.0 * f0 - 4.0 * fm1 + fm2) * c.q25y;
-        double t2 = v * (-fp2 + 8.0 * fp1 - 8.0 * fm1 + fm2) * c.c12y;
+    if (Pe > R(2) && Pe < R(50)) {
+        R t1 = abs(v) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25y;
+        R t2 = v * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12y;
         return t1 + t2;
     }
-    return v * ((fm2 - 8.0 * fm1 + 8.0 * fp1 - fp2) * c.c12y);
+    return v * ((fm2 - R(8) * fm1 + R(8) * fp1 - fp2) * c.c12y);
 }
 
 // xi: Pe from the physical spacing, window 2 < Pe < 5 (:690-713)
-__device__ __forceinline__ double conv_z(double w, double dz, bool nearb, double fm2, double fm1, double f0,
-                                         double fp1, double fp2, const ConvCoef& c) {
-    double sgn = w > -1.0 ? 1.0 : -1.0;
-    double Pe = (sgn * c.tf * w * dz);
+template <typename R>
+__device__ __forceinline__ R conv_z(R w, R dz, bool nearb, R fm2, R fm1, R f0, R fp1, R fp2,
+                                    const ConvCoef<R>& c) {
+    R sgn = w > R(-1) ? R(1) : R(-1);
+    R Pe = (sgn * c.tf * w * dz);
     if (nearb) return (w * (fp1 - fm1) * c.h05z);
-    if (Pe > 2.0 && Pe < 5.0) {
-        double t1 = fabs(w) * (fp2 - 4.0 * fp1 + 6.0 * f0 - 4.0 * fm1 + fm2) * c.q25z;
-        double t2 = w * (-fp2 + 8.0 * fp1 - 8.0 * fm1 + fm2) * c.c12z;
+    if (Pe > R(2) && Pe < R(5)) {
+        R t1 = abs(w) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25z;
+        R t2 = w * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12z;
         return t1 + t2;
     }
-    return w * ((fm2 - 8.0 * fm1 + 8.0 * fp1 - fp2) * c.c12z);
+    return w * ((fm2 - R(8) * fm1 + R(8) * fp1 - fp2) * c.c12z);
 }
 
 // conv(i,j,k,1..3) and Q(i,j,k,1..3) (dnstbl2/dnstbl.f90:621-768), fused:
 // conv is never stored.  One thread per interior point.
-__global__ void __launch_bounds__(128) k_conv_q(Geom g, ConvCoef c, const double* __restrict__ U1,
-                                                const double* __restrict__ U2, const double* __restrict__ U3,
-                                                const double* __restrict__ Pr, const double* __restrict__ x3,
-                                                const double* __restrict__ jacinv, double* __restrict__ Q1,
-                                                double* __restrict__ Q2, double* __restrict__ Q3) {
+template <typename T>
+__global__ void __launch_bounds__(128) k_conv_q(Geom g, ConvCoef<T> c, const T* __restrict__ U1,
+                                                const T* __restrict__ U2, const T* __restrict__ U3,
+                                                const T* __restrict__ Pr, const double* __restrict__ x3,
+                                                const double* __restrict__ jacinv, T* __restrict__ Q1,
+                                                T* __restrict__ Q2, T* __restrict__ Q3) {
     int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
@@ -141,30 +148,30 @@ __global__ void __launch_bounds__(128) k_conv_q(Geom g, ConvCoef c, const double
     const bool nbx = (i <= 1) || (i >= g.nx - 2);
     const bool nby = (j == 1) || (j == g.ny - 2);
     const bool nbz = (k <= 1) || (k >= g.nz - 2);
-    const double u = U1[p], v = U2[p], w = U3[p];
-    const double dz = x3[k + 1] - x3[k];
-    const double jk = jacinv[k];
-    const double* Fs[3] = {U1, U2, U3};
-    double conv[3];
+    const T u = U1[p], v = U2[p], w = U3[p];
+    const T dz = (T)(x3[k + 1] - x3[k]);
+    const T jk = (T)jacinv[k];
+    const T* Fs[3] = {U1, U2, U3};
+    T conv[3];
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
-        const double* F = Fs[cc];
-        double f0 = F[p];
-        double d1 = conv_x(u, nbx, nbx ? 0.0 : F[p - 2], F[p - 1], f0, F[p + 1], nbx ? 0.0 : F[p + 2], c);
-        double d2 = conv_y(v, nby, F[pjm2], F[pjm1], f0, F[pjp1], F[pjp2], c);
-        double d3 = conv_z(w, dz, nbz, nbz ? 0.0 : F[p - 2 * sz], F[p - sz], f0, F[p + sz],
-                           nbz ? 0.0 : F[p + 2 * sz], c);
+        const T* F = Fs[cc];
+        T f0 = F[p];
+        T d1 = conv_x<T>(u, nbx, nbx ? T(0) : F[p - 2], F[p - 1], f0, F[p + 1], nbx ? T(0) : F[p + 2], c);
+        T d2 = conv_y<T>(v, nby, F[pjm2], F[pjm1], f0, F[pjp1], F[pjp2], c);
+        T d3 = conv_z<T>(w, dz, nbz, nbz ? T(0) : F[p - 2 * sz], F[p - sz], f0, F[p + sz],
+                           nbz ? T(0) : F[p + 2 * sz], c);
         conv[cc] = d1 + d2 + (d3 * jk);
     }
     (void)sy;
-    double g1 = 0.5 * (Pr[p + 1] - Pr[p - 1]) * c.invdx;
-    double g2 = 0.5 * (Pr[pjp1] - Pr[pjm1]) * c.invdy;
-    double g3 = 0.5 * (Pr[p + sz] - Pr[p - sz]) * (c.invdxi * jk);
-    double q5 = u + (c.dt * (0.0 - conv[0]));
+    T g1 = T(0.5) * (Pr[p + 1] - Pr[p - 1]) * c.invdx;
+    T g2 = T(0.5) * (Pr[pjp1] - Pr[pjm1]) * c.invdy;
+    T g3 = T(0.5) * (Pr[p + sz] - Pr[p - sz]) * (c.invdxi * jk);
+    T q5 = u + (c.dt * (T(0) - conv[0]));
     Q1[p] = q5 - (c.dt * g1);
-    double q6 = v + (c.dt * (0.0 - conv[1]));
+    T q6 = v + (c.dt * (T(0) - conv[1]));
     Q2[p] = q6 - (c.dt * g2);
-    double q7 = w + (c.dt * (0.0 - conv[2]));
+    T q7 = w + (c.dt * (T(0) - conv[2]));
     Q3[p] = q7 - (c.dt * g3);
 }
 
@@ -176,18 +183,19 @@ struct GsCoef {
     double cE, cW, cN, cS;  // t*Av{e,w,n,s}, t = -dt/Re
 };
 
+template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, const double* __restrict__ Ab,
                                                           const double* __restrict__ At,
                                                           const double* __restrict__ Ap, double t,
-                                                          const double* __restrict__ U0, const double* __restrict__ U1,
-                                                          const double* __restrict__ U2, const double* __restrict__ Q0,
-                                                          const double* __restrict__ Q1, const double* __restrict__ Q2,
+                                                          const T* __restrict__ U0, const T* __restrict__ U1,
+                                                          const T* __restrict__ U2, const T* __restrict__ Q0,
+                                                          const T* __restrict__ Q1, const T* __restrict__ Q2,
                                                           int3 comps, int ncomp, RedWork rw, DevScalars* sc) {
     __shared__ double s_red[RED_THREADS / 32];
     const int cid = blockIdx.y;
     const int comp = cid == 0 ? comps.x : (cid == 1 ? comps.y : comps.z);
-    const double* F = comp == 0 ? U0 : (comp == 1 ? U1 : U2);
-    const double* Qc = comp == 0 ? Q0 : (comp == 1 ? Q1 : Q2);
+    const T* F = comp == 0 ? U0 : (comp == 1 ? U1 : U2);
+    const T* Qc = comp == 0 ? Q0 : (comp == 1 ? Q1 : Q2);
     const int ni = g.nx - 2, J = g.ny - 2, nk = g.nz - 2;
     const long long n = (long long)ni * J * nk;
     double acc = 0.0;
@@ -198,11 +206,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, con
         int j = 1 + (int)(r % J);
         int k = 1 + (int)(r / J);
         long long p = idx(g, i, j, k);
-        double d = 1.0 + (t * Ap[k]);
-        double cT = t * At[k], cB = t * Ab[k];
-        double res = Qc[p] - d * F[p] - gc.cE * F[p + 1] - gc.cW * F[p - 1] - gc.cN * F[idx(g, i, jp1(g, j), k)] -
-                     gc.cS * F[idx(g, i, jm1(g, j), k)] - cT * F[p + g.ps] - cB * F[p - g.ps];
-        acc += fabs(res);
+        const T d = (T)(1.0 + (t * Ap[k]));
+        const T cT = (T)(t * At[k]), cB = (T)(t * Ab[k]);
+        const T cE = (T)gc.cE, cW = (T)gc.cW, cN = (T)gc.cN, cS = (T)gc.cS;
+        T res = Qc[p] - d * F[p] - cE * F[p + 1] - cW * F[p - 1] - cN * F[idx(g, i, jp1(g, j), k)] -
+                cS * F[idx(g, i, jm1(g, j), k)] - cT * F[p + g.ps] - cB * F[p - g.ps];
+        acc += fabs((double)res);
     }
     double bt = block_sum(acc, s_red);
     grid_finish(bt, rw, comp, gridDim.x, blockIdx.x, &sc->red[comp], 0);
@@ -210,17 +219,21 @@ __global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, con
 
 // ------------------------------------------------------------ divergence
 // Q8 = div(U*)/dt (dnstbl2/dnstbl.f90:905-935)
+template <typename T>
 __global__ void __launch_bounds__(128) k_div(Geom g, double invdx, double invdy, double dt,
-                                             const double* __restrict__ U1, const double* __restrict__ U2,
-                                             const double* __restrict__ U3, const double* __restrict__ x3,
+                                             const T* __restrict__ U1, const T* __restrict__ U2,
+                                             const T* __restrict__ U3, const double* __restrict__ x3,
                                              double* __restrict__ Q8) {
     int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
     long long p = idx(g, i, j, k);
-    double d1 = (((U1[p + 1] + U1[p]) * 0.5) - (((U1[p] + U1[p - 1]) * 0.5))) * invdx;
-    double d2 = (((U2[idx(g, i, jp1(g, j), k)] + U2[p]) * 0.5) - (((U2[p] + U2[idx(g, i, jm1(g, j), k)]) * 0.5))) * invdy;
-    double d3 = 2.0 * (((U3[p + g.ps] + U3[p]) * 0.5) - (((U3[p] + U3[p - g.ps]) * 0.5))) / (x3[k + 1] - x3[k - 1]);
+    const double u0 = U1[p], v0 = U2[p], w0 = U3[p];
+    double d1 = ((((double)U1[p + 1] + u0) * 0.5) - (((u0 + (double)U1[p - 1]) * 0.5))) * invdx;
+    double d2 = ((((double)U2[idx(g, i, jp1(g, j), k)] + v0) * 0.5) -
+                 (((v0 + (double)U2[idx(g, i, jm1(g, j), k)]) * 0.5))) * invdy;
+    double d3 = 2.0 * ((((double)U3[p + g.ps] + w0) * 0.5) - (((w0 + (double)U3[p - g.ps]) * 0.5))) /
+                (x3[k + 1] - x3[k - 1]);
     Q8[p] = (d1 + d2 + d3) / dt;
 }
 
@@ -281,49 +294,54 @@ __global__ void k_pc_bc_inout(Geom g, double* __restrict__ PC) {
 }
 
 // P += p', U -= dt grad p' (dnstbl2/dnstbl.f90:1268-1314)
+template <typename T>
 __global__ void __launch_bounds__(128) k_project(Geom g, double invdx, double invdy, double invdxi, double dt,
                                                  const double* __restrict__ jacinv, const double* __restrict__ PC,
-                                                 double* __restrict__ Pr, double* __restrict__ U1,
-                                                 double* __restrict__ U2, double* __restrict__ U3) {
+                                                 T* __restrict__ Pr, T* __restrict__ U1,
+                                                 T* __restrict__ U2, T* __restrict__ U3) {
     int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
     long long p = idx(g, i, j, k);
-    Pr[p] = Pr[p] + PC[p];
+    Pr[p] = (T)((double)Pr[p] + PC[p]);
     double g1 = 0.5 * (PC[p + 1] - PC[p - 1]) * (invdx);
     double g2 = 0.5 * (PC[idx(g, i, jp1(g, j), k)] - PC[idx(g, i, jm1(g, j), k)]) * (invdy);
     double g3 = 0.5 * (PC[p + g.ps] - PC[p - g.ps]) * (invdxi * jacinv[k]);
-    U1[p] = U1[p] - (dt * g1);
-    U2[p] = U2[p] - (dt * g2);
-    U3[p] = U3[p] - (dt * g3);
+    U1[p] = (T)((double)U1[p] - (dt * g1));
+    U2[p] = (T)((double)U2[p] - (dt * g2));
+    U3[p] = (T)((double)U3[p] - (dt * g3));
 }
 
 // velocity BCs, wall and top (:1317-1330), one thread per (i, j unique)
-__global__ void k_vel_bc_walltop(Geom g, double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3) {
+template <typename T>
+__global__ void k_vel_bc_walltop(Geom g, T* __restrict__ U1, T* __restrict__ U2, T* __restrict__ U3) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int J = g.ny - 2;
     if (t >= g.nx * J) return;
     int i = t % g.nx, j = 1 + t / g.nx;
     int nz = g.nz;
-    double* Us[3] = {U1, U2, U3};
+    T* Us[3] = {U1, U2, U3};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) Us[c][idx(g, i, j, 0)] = 0.0;
+    for (int c = 0; c < 3; ++c) Us[c][idx(g, i, j, 0)] = T(0);
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-        Us[c][idx(g, i, j, nz - 1)] = (4.0 * Us[c][idx(g, i, j, nz - 2)] - Us[c][idx(g, i, j, nz - 3)]) / 3.0;
+        Us[c][idx(g, i, j, nz - 1)] =
+            (T)((4.0 * (double)Us[c][idx(g, i, j, nz - 2)] - (double)Us[c][idx(g, i, j, nz - 3)]) / 3.0);
 }
 
 // outflow (:1342), one thread per (j unique, k all)
-__global__ void k_vel_bc_out(Geom g, double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3) {
+template <typename T>
+__global__ void k_vel_bc_out(Geom g, T* __restrict__ U1, T* __restrict__ U2, T* __restrict__ U3) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int J = g.ny - 2;
     if (t >= J * g.nz) return;
     int j = 1 + t % J, k = t / J;
     int nx = g.nx;
-    double* Us[3] = {U1, U2, U3};
+    T* Us[3] = {U1, U2, U3};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-        Us[c][idx(g, nx - 1, j, k)] = (4.0 * Us[c][idx(g, nx - 2, j, k)] - Us[c][idx(g, nx - 3, j, k)]) / 3.0;
+        Us[c][idx(g, nx - 1, j, k)] =
+            (T)((4.0 * (double)Us[c][idx(g, nx - 2, j, k)] - (double)Us[c][idx(g, nx - 3, j, k)]) / 3.0);
 }
 
 struct PbcCoef {
@@ -332,10 +350,26 @@ struct PbcCoef {
 
 // pressure BCs (:1352-1461): wall, top, outflow, inflow -- independent of
 // each other, one flat index space.
-__global__ void k_press_bc(Geom g, PbcCoef c, const double* __restrict__ U1, const double* __restrict__ U2,
-                           const double* __restrict__ U3, const double* __restrict__ uold1,
+template <typename T>
+__global__ void k_press_bc(Geom g, PbcCoef c, const T* __restrict__ U1p, const T* __restrict__ U2p,
+                           const T* __restrict__ U3p, const double* __restrict__ uold1,
                            const double* __restrict__ jacinv, const double* __restrict__ jac2,
-                           double* __restrict__ Pr) {
+                           T* __restrict__ Prp) {
+    struct Rd {
+        const T* p;
+        __device__ double operator[](long long q) const { return (double)p[q]; }
+    };
+    struct Wr {
+        T* p;
+        struct Ref {
+            T* a;
+            __device__ void operator=(double v) { *a = (T)v; }
+            __device__ operator double() const { return (double)*a; }
+        };
+        __device__ Ref operator[](long long q) const { return Ref{p + q}; }
+    };
+    const Rd U1{U1p}, U2{U2p}, U3{U3p};
+    const Wr Pr{Prp};
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = g.nx, ny = g.ny, nz = g.nz, J = ny - 2, I = nx - 2, K = nz - 2;
     const long long nW = (long long)I * J, nO = (long long)J * K;
@@ -400,8 +434,9 @@ __global__ void k_press_bc(Geom g, PbcCoef c, const double* __restrict__ U1, con
 }
 
 // spanwise periodic copies of U and P (:1465-1469), one thread per (i,k)
-__global__ void k_periodic(Geom g, double* __restrict__ U1, double* __restrict__ U2, double* __restrict__ U3,
-                           double* __restrict__ Pr) {
+template <typename T>
+__global__ void k_periodic(Geom g, T* __restrict__ U1, T* __restrict__ U2, T* __restrict__ U3,
+                           T* __restrict__ Pr) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.nx * g.nz) return;
     int i = t % g.nx, k = t / g.nx;
@@ -414,9 +449,10 @@ __global__ void k_periodic(Geom g, double* __restrict__ U1, double* __restrict__
 
 // -------------------------------------------- diagnostics: divergence print
 // (dnstbl2/dnstbl.f90:1526-1577): sum of the 4th-order divergence -> red[3]
+template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_div_diag(Geom g, double invdx, double invdy, double invdxi,
-                                                          const double* __restrict__ U1, const double* __restrict__ U2,
-                                                          const double* __restrict__ U3,
+                                                          const T* __restrict__ U1, const T* __restrict__ U2,
+                                                          const T* __restrict__ U3,
                                                           const double* __restrict__ jacinv, RedWork rw,
                                                           DevScalars* sc, int slot) {
     __shared__ double s_red[RED_THREADS / 32];
@@ -432,16 +468,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_div_diag(Geom g, double invdx, 
         int k = 1 + (int)(r / J);
         long long p = idx(g, i, j, k);
         double d1, d2, d3;
-        if (i == 1 || i == g.nx - 2) d1 = (U1[p + 1] - U1[p - 1]) * (0.5 * invdx);
-        else d1 = ((U1[p - 2] - 8.0 * U1[p - 1] + 8.0 * U1[p + 1] - U1[p + 2]) * (c12 * invdx));
+        if (i == 1 || i == g.nx - 2) d1 = ((double)U1[p + 1] - (double)U1[p - 1]) * (0.5 * invdx);
+        else d1 = (((double)U1[p - 2] - 8.0 * (double)U1[p - 1] + 8.0 * (double)U1[p + 1] - (double)U1[p + 2]) * (c12 * invdx));
         if (j == 1 || j == g.ny - 2)
-            d2 = (U2[idx(g, i, jp1(g, j), k)] - U2[idx(g, i, jm1(g, j), k)]) * (0.5 * invdy);
+            d2 = ((double)U2[idx(g, i, jp1(g, j), k)] - (double)U2[idx(g, i, jm1(g, j), k)]) * (0.5 * invdy);
         else
-            d2 = ((U2[idx(g, i, jm2(g, j), k)] - 8.0 * U2[idx(g, i, jm1(g, j), k)] +
-                   8.0 * U2[idx(g, i, jp1(g, j), k)] - U2[idx(g, i, jp2(g, j), k)]) *
+            d2 = (((double)U2[idx(g, i, jm2(g, j), k)] - 8.0 * (double)U2[idx(g, i, jm1(g, j), k)] +
+                   8.0 * (double)U2[idx(g, i, jp1(g, j), k)] - (double)U2[idx(g, i, jp2(g, j), k)]) *
                   (c12 * invdy));
-        if (k <= 1 || k >= g.nz - 2) d3 = ((U3[p + g.ps] - U3[p - g.ps]) * (0.5 * invdxi));
-        else d3 = ((U3[p - 2 * g.ps] - 8.0 * U3[p - g.ps] + 8.0 * U3[p + g.ps] - U3[p + 2 * g.ps]) * (c12 * invdxi));
+        if (k <= 1 || k >= g.nz - 2) d3 = (((double)U3[p + g.ps] - (double)U3[p - g.ps]) * (0.5 * invdxi));
+        else d3 = (((double)U3[p - 2 * g.ps] - 8.0 * (double)U3[p - g.ps] + 8.0 * (double)U3[p + g.ps] -
+                    (double)U3[p + 2 * g.ps]) * (c12 * invdxi));
         acc += (d1 + d2 + (d3 * jacinv[k]));
     }
     double bt = block_sum(acc, s_red);
@@ -451,8 +488,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_div_diag(Geom g, double invdx, 
 // -------------------------- per-step fluctuations, KE, blowup (:1707-1775)
 // Ufluc = U - means on every slab's planes; only the recycling plane irec is
 // kept (ufl_live); KE sum -> red[slot]; max fluctuation -> red[slot+1].
-__global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const double* __restrict__ U1,
-                                                         const double* __restrict__ U2, const double* __restrict__ U3,
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const T* __restrict__ U1,
+                                                         const T* __restrict__ U2, const T* __restrict__ U3,
                                                          const double* __restrict__ usum2,
                                                          const double* __restrict__ vsum2,
                                                          const double* __restrict__ wsum2, double* __restrict__ ufl_live,
@@ -470,7 +508,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const double* _
         int k = 1 + (int)(r / J);
         long long p = idx(g, i, j, k);
         size_t q = (size_t)i + (size_t)nx * k;
-        double f1 = U1[p] - usum2[q], f2 = U2[p] - vsum2[q], f3 = U3[p] - wsum2[q];
+        double f1 = (double)U1[p] - usum2[q], f2 = (double)U2[p] - vsum2[q], f3 = (double)U3[p] - wsum2[q];
         acc += f1 * f1 + f2 * f2 + f3 * f3;
         mx = fmax(mx, fmax(f1, fmax(f2, f3)));
         if (i == irec0) {
@@ -492,17 +530,18 @@ __global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const double* _
 
 // ------------------------------------------- statistics (:1902-1993)
 // one thread per (i,k), k over all planes 0..nz-1, spanwise sums in row order
-__global__ void k_stats(Geom g, double dA, double A, const double* __restrict__ U1, const double* __restrict__ U2,
-                        const double* __restrict__ U3, double* __restrict__ sums) {
+template <typename T>
+__global__ void k_stats(Geom g, double dA, double A, const T* __restrict__ U1, const T* __restrict__ U2,
+                        const T* __restrict__ U3, double* __restrict__ sums) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.nx * g.nz) return;
     int i = t % g.nx, k = t / g.nx;
     double tu = 0, tv = 0, tw = 0, tuu = 0, tvv = 0, tww = 0, tuv = 0, tuw = 0, tvw = 0;
     for (int j = 1; j <= g.ny - 2; ++j) {
         long long p = idx(g, i, j, k), pp = idx(g, i, jp1(g, j), k);
-        double su = 0.50 * (U1[p] + U1[pp]);
-        double sv = 0.50 * (U2[p] + U2[pp]);
-        double sw = 0.50 * (U3[p] + U3[pp]);
+        double su = 0.50 * ((double)U1[p] + (double)U1[pp]);
+        double sv = 0.50 * ((double)U2[p] + (double)U2[pp]);
+        double sw = 0.50 * ((double)U3[p] + (double)U3[pp]);
         tu = tu + (su * dA); tv = tv + (sv * dA); tw = tw + (sw * dA);
         tuu = tuu + (su * su * dA); tvv = tvv + (sv * sv * dA); tww = tww + (sw * sw * dA);
         tuv = tuv + (su * sv * dA); tuw = tuw + (su * sw * dA); tvw = tvw + (sv * sw * dA);
@@ -584,8 +623,9 @@ __global__ void k_rescale(Geom g, int irec0, double cum, double ue, double re, c
 }
 
 // refresh Ufluc(irec,:,k,:) with the new means and zero the sums (:2341-2365)
-__global__ void k_rescale_tail(Geom g, int irec0, const double* __restrict__ U1, const double* __restrict__ U2,
-                               const double* __restrict__ U3, const double* __restrict__ usum2,
+template <typename T>
+__global__ void k_rescale_tail(Geom g, int irec0, const T* __restrict__ U1, const T* __restrict__ U2,
+                               const T* __restrict__ U3, const double* __restrict__ usum2,
                                const double* __restrict__ vsum2, const double* __restrict__ wsum2,
                                double* __restrict__ ufl_live, double* __restrict__ sums) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -595,9 +635,9 @@ __global__ void k_rescale_tail(Geom g, int irec0, const double* __restrict__ U1,
         int j = 1 + t % J, k = 1 + t / J;
         long long p = idx(g, irec0, j, k);
         size_t q = (size_t)irec0 + (size_t)g.nx * k, pl = (size_t)g.ny * g.nz, pj = (size_t)j + (size_t)g.ny * k;
-        ufl_live[pj] = U1[p] - usum2[q];
-        ufl_live[pl + pj] = U2[p] - vsum2[q];
-        ufl_live[2 * pl + pj] = U3[p] - wsum2[q];
+        ufl_live[pj] = (double)U1[p] - usum2[q];
+        ufl_live[pl + pj] = (double)U2[p] - vsum2[q];
+        ufl_live[2 * pl + pj] = (double)U3[p] - wsum2[q];
     }
     for (size_t q = t; q < 9 * n2; q += (size_t)gridDim.x * blockDim.x) sums[q] = 0.0;
 }
@@ -608,11 +648,13 @@ __global__ void k_rescale_tail(Geom g, int irec0, const double* __restrict__ U1,
 static inline dim3 interior_grid(const Geom& g) {
     return dim3((g.nx - 2 + 127) / 128, g.ny - 2, g.nz - 2);
 }
+static inline bool mixed(const tbl_handle* h) { return h->cfg.precision == TBL_PREC_MIXED; }
 
 int launch_save_uold(tbl_handle* h) {
     const Geom& g = h->g;
     int n = g.ny * g.nz;
-    k_save_uold<<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->U[0], h->uold1);
+    if (mixed(h)) k_save_uold<float><<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->Uf[0], h->uold1);
+    else k_save_uold<double><<<(n + 255) / 256, 256, 0, h->stream>>>(g, h->U[0], h->uold1);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -620,48 +662,119 @@ int launch_save_uold(tbl_handle* h) {
 int launch_inflow(tbl_handle* h) {
     const Geom& g = h->g;
     int n = (g.ny - 2) * (g.nz - 2);
-    k_inflow<<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2, h->wsum2,
-                                                      h->wt, h->ume1, h->newk, h->ufl_file, h->ufl_live, h->slab_of_k,
-                                                      h->slabs, h->sc, h->cfg.irec - 1, h->cfg.ue);
+    if (mixed(h))
+        k_inflow<float><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2, h->vsum2,
+                                                                 h->wsum2, h->wt, h->ume1, h->newk, h->ufl_file,
+                                                                 h->ufl_live, h->slab_of_k, h->slabs, h->sc,
+                                                                 h->cfg.irec - 1, h->cfg.ue);
+    else
+        k_inflow<double><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2,
+                                                                  h->wsum2, h->wt, h->ume1, h->newk, h->ufl_file,
+                                                                  h->ufl_live, h->slab_of_k, h->slabs, h->sc,
+                                                                  h->cfg.irec - 1, h->cfg.ue);
     LAUNCH_COUNT(h);
     return TBL_OK;
+}
+
+template <typename R>
+static ConvCoef<R> conv_coef(const tbl_config& c) {
+    ConvCoef<R> cc;
+    const double invdx = 1.0 / c.dx, invdy = 1.0 / c.dy, invdxi = 1.0 / c.dxi, c12 = 1.0 / 12.0;
+    cc.tf = (R)c.re; cc.dx = (R)c.dx; cc.dy = (R)c.dy;
+    cc.invdx = (R)invdx; cc.invdy = (R)invdy; cc.invdxi = (R)invdxi;
+    cc.inv2dx = (R)(1.0 / (2.0 * c.dx));
+    cc.c12x = (R)(c12 * invdx); cc.c12y = (R)(c12 * invdy); cc.c12z = (R)(c12 * invdxi);
+    cc.q25x = (R)(0.25 * invdx); cc.q25y = (R)(0.25 * invdy); cc.q25z = (R)(0.25 * invdxi);
+    cc.h05z = (R)(0.5 * invdxi);
+    cc.dt = (R)c.dt;
+    return cc;
 }
 
 int launch_conv_q(tbl_handle* h) {
     const Geom& g = h->g;
-    const tbl_config& c = h->cfg;
-    ConvCoef cc;
-    cc.tf = c.re; cc.dx = c.dx; cc.dy = c.dy;
-    cc.invdx = 1.0 / c.dx; cc.invdy = 1.0 / c.dy; cc.invdxi = 1.0 / c.dxi;
-    cc.inv2dx = 1.0 / (2.0 * c.dx);
-    const double c12 = 1.0 / 12.0;
-    cc.c12x = c12 * cc.invdx; cc.c12y = c12 * cc.invdy; cc.c12z = c12 * cc.invdxi;
-    cc.q25x = 0.25 * cc.invdx; cc.q25y = 0.25 * cc.invdy; cc.q25z = 0.25 * cc.invdxi;
-    cc.h05z = 0.5 * cc.invdxi;
-    cc.dt = c.dt;
-    k_conv_q<<<interior_grid(g), 128, 0, h->stream>>>(g, cc, h->U[0], h->U[1], h->U[2], h->Pr, h->x3, h->jacinv,
-                                                      h->Q[0], h->Q[1], h->Q[2]);
+    if (mixed(h))
+        k_conv_q<float><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<float>(h->cfg), h->Uf[0], h->Uf[1],
+                                                                 h->Uf[2], h->Pf, h->x3, h->jacinv, h->Qf[0],
+                                                                 h->Qf[1], h->Qf[2]);
+    else
+        k_conv_q<double><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<double>(h->cfg), h->U[0], h->U[1],
+                                                                  h->U[2], h->Pr, h->x3, h->jacinv, h->Q[0], h->Q[1],
+                                                                  h->Q[2]);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
 
+// GS residual of the listed components.  In mixed precision the iteration is
+// on the increment D (delta form) with right-hand side r0 stored in Qf.
 int launch_gs_resid(tbl_handle* h, const int* comps, int ncomp, int nblocks) {
     const Geom& g = h->g;
     const double t = -h->cfg.dt / (h->cfg.re);
     const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
     GsCoef gc{t * aw, t * aw, t * as, t * as};
     int3 cs = make_int3(comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0);
-    k_gs_resid<<<dim3(nblocks, ncomp), RED_THREADS, 0, h->stream>>>(g, gc, h->Ab, h->At, h->Ap, t, h->U[0], h->U[1],
-                                                                     h->U[2], h->Q[0], h->Q[1], h->Q[2], cs, ncomp,
-                                                                     h->red, h->sc);
+    if (mixed(h))
+        k_gs_resid<float><<<dim3(nblocks, ncomp), RED_THREADS, 0, h->stream>>>(
+            g, gc, h->Ab, h->At, h->Ap, t, h->Df[0], h->Df[1], h->Df[2], h->Qf[0], h->Qf[1], h->Qf[2], cs, ncomp,
+            h->red, h->sc);
+    else
+        k_gs_resid<double><<<dim3(nblocks, ncomp), RED_THREADS, 0, h->stream>>>(
+            g, gc, h->Ab, h->At, h->Ap, t, h->U[0], h->U[1], h->U[2], h->Q[0], h->Q[1], h->Q[2], cs, ncomp, h->red,
+            h->sc);
+    LAUNCH_COUNT(h);
+    return TBL_OK;
+}
+
+// Mixed precision: r0 = Q - (I + t L7) U in place of Q, D = 0 (start of the
+// delta-form GS; same iterates as GS on U from U^n, rounding on the small D).
+__global__ void __launch_bounds__(128) k_gs_delta_init(Geom g, double t, double aw, double as,
+                                                       const double* __restrict__ Ab, const double* __restrict__ At,
+                                                       const double* __restrict__ Ap, const float* __restrict__ U,
+                                                       float* __restrict__ Q, float* __restrict__ D) {
+    int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    if (i > g.nx - 2) return;
+    long long p = idx(g, i, j, k);
+    const float d = (float)(1.0 + t * Ap[k]), cE = (float)(t * aw), cN = (float)(t * as);
+    const float cT = (float)(t * At[k]), cB = (float)(t * Ab[k]);
+    float r = Q[p] - d * U[p] - cE * U[p + 1] - cE * U[p - 1] - cN * U[idx(g, i, jp1(g, j), k)] -
+              cN * U[idx(g, i, jm1(g, j), k)] - cT * U[p + g.ps] - cB * U[p - g.ps];
+    Q[p] = r;
+    D[p] = 0.0f;
+}
+
+// U += D on the interior (end of the delta-form GS)
+__global__ void __launch_bounds__(128) k_gs_delta_apply(Geom g, const float* __restrict__ D, float* __restrict__ U) {
+    int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    if (i > g.nx - 2) return;
+    long long p = idx(g, i, j, k);
+    U[p] = U[p] + D[p];
+}
+
+int launch_gs_delta_init(tbl_handle* h, int comp) {
+    const Geom& g = h->g;
+    const double t = -h->cfg.dt / (h->cfg.re);
+    k_gs_delta_init<<<interior_grid(g), 128, 0, h->stream>>>(g, t, 1.0 / (h->cfg.dx * h->cfg.dx),
+                                                            1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap,
+                                                            h->Uf[comp], h->Qf[comp], h->Df[comp]);
+    LAUNCH_COUNT(h);
+    return TBL_OK;
+}
+
+int launch_gs_delta_apply(tbl_handle* h, int comp) {
+    k_gs_delta_apply<<<interior_grid(h->g), 128, 0, h->stream>>>(h->g, h->Df[comp], h->Uf[comp]);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
 
 int launch_div(tbl_handle* h) {
     const Geom& g = h->g;
-    k_div<<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy, h->cfg.dt, h->U[0], h->U[1],
-                                                   h->U[2], h->x3, h->Q8);
+    if (mixed(h))
+        k_div<float><<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy, h->cfg.dt,
+                                                              h->Uf[0], h->Uf[1], h->Uf[2], h->x3, h->Q8);
+    else
+        k_div<double><<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy, h->cfg.dt,
+                                                               h->U[0], h->U[1], h->U[2], h->x3, h->Q8);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -674,33 +787,45 @@ int launch_pc_zero_faces(tbl_handle* h) {
     return TBL_OK;
 }
 
-int launch_project_bcs(tbl_handle* h) {
+template <typename T>
+static void project_bcs_t(tbl_handle* h, T* U0, T* U1, T* U2, T* Pr) {
     const Geom& g = h->g;
     const tbl_config& c = h->cfg;
     int n1 = g.nx * (g.ny - 2), n2 = g.nx * g.nz, n3 = (g.ny - 2) * g.nz;
     k_pc_bc_walltop<<<(n1 + 255) / 256, 256, 0, h->stream>>>(g, h->PC);
     k_pc_periodic<<<(n2 + 255) / 256, 256, 0, h->stream>>>(g, h->PC);
     k_pc_bc_inout<<<(n3 + 255) / 256, 256, 0, h->stream>>>(g, h->PC);
-    k_project<<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / c.dx, 1.0 / c.dy, 1.0 / c.dxi, c.dt, h->jacinv,
-                                                       h->PC, h->Pr, h->U[0], h->U[1], h->U[2]);
-    k_vel_bc_walltop<<<(n1 + 255) / 256, 256, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2]);
-    k_vel_bc_out<<<(n3 + 255) / 256, 256, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2]);
+    k_project<T><<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / c.dx, 1.0 / c.dy, 1.0 / c.dxi, c.dt, h->jacinv,
+                                                          h->PC, Pr, U0, U1, U2);
+    k_vel_bc_walltop<T><<<(n1 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2);
+    k_vel_bc_out<T><<<(n3 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2);
     PbcCoef pc;
     pc.dx = c.dx; pc.dy = c.dy; pc.dxi = c.dxi; pc.re = c.re; pc.dt = c.dt;
     pc.df1 = h->x3h[1] - h->x3h[0];
     pc.df2 = h->x3h[2] - h->x3h[0];
     long long np = 2LL * (g.nx - 2) * (g.ny - 2) + 2LL * (g.ny - 2) * (g.nz - 2);
-    k_press_bc<<<(unsigned)((np + 255) / 256), 256, 0, h->stream>>>(g, pc, h->U[0], h->U[1], h->U[2], h->uold1,
-                                                                    h->jacinv, h->jac2, h->Pr);
-    k_periodic<<<(n2 + 255) / 256, 256, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->Pr);
+    k_press_bc<T><<<(unsigned)((np + 255) / 256), 256, 0, h->stream>>>(g, pc, U0, U1, U2, h->uold1, h->jacinv,
+                                                                       h->jac2, Pr);
+    k_periodic<T><<<(n2 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2, Pr);
     h->launches += 8;
+}
+
+int launch_project_bcs(tbl_handle* h) {
+    if (mixed(h)) project_bcs_t<float>(h, h->Uf[0], h->Uf[1], h->Uf[2], h->Pf);
+    else project_bcs_t<double>(h, h->U[0], h->U[1], h->U[2], h->Pr);
     return TBL_OK;
 }
 
 int launch_div_diag(tbl_handle* h, int nblocks, int slot) {
     const Geom& g = h->g;
-    k_div_diag<<<nblocks, RED_THREADS, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy, 1.0 / h->cfg.dxi,
-                                                       h->U[0], h->U[1], h->U[2], h->jacinv, h->red, h->sc, slot);
+    if (mixed(h))
+        k_div_diag<float><<<nblocks, RED_THREADS, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy,
+                                                                  1.0 / h->cfg.dxi, h->Uf[0], h->Uf[1], h->Uf[2],
+                                                                  h->jacinv, h->red, h->sc, slot);
+    else
+        k_div_diag<double><<<nblocks, RED_THREADS, 0, h->stream>>>(g, 1.0 / h->cfg.dx, 1.0 / h->cfg.dy,
+                                                                   1.0 / h->cfg.dxi, h->U[0], h->U[1], h->U[2],
+                                                                   h->jacinv, h->red, h->sc, slot);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -708,8 +833,14 @@ int launch_div_diag(tbl_handle* h, int nblocks, int slot) {
 int launch_fluc_ke(tbl_handle* h, int nblocks, int slot) {
     const Geom& g = h->g;
     TBL_CUDA_TRY(cudaMemsetAsync(&h->sc->red[slot + 1], 0, sizeof(double), h->stream));
-    k_fluc_ke<<<nblocks, RED_THREADS, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2, h->wsum2,
-                                                      h->ufl_live, h->cfg.irec - 1, h->red, h->sc, slot);
+    if (mixed(h))
+        k_fluc_ke<float><<<nblocks, RED_THREADS, 0, h->stream>>>(g, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2,
+                                                                 h->vsum2, h->wsum2, h->ufl_live, h->cfg.irec - 1,
+                                                                 h->red, h->sc, slot);
+    else
+        k_fluc_ke<double><<<nblocks, RED_THREADS, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2,
+                                                                  h->wsum2, h->ufl_live, h->cfg.irec - 1, h->red,
+                                                                  h->sc, slot);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -717,8 +848,12 @@ int launch_fluc_ke(tbl_handle* h, int nblocks, int slot) {
 int launch_stats(tbl_handle* h) {
     const Geom& g = h->g;
     int n = g.nx * g.nz;
-    // A = x2(ny) - x2(2), dA = dy (:437-442)
-    k_stats<<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->cfg.dy, h->stats_A, h->U[0], h->U[1], h->U[2], h->sums);
+    if (mixed(h))
+        k_stats<float><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->cfg.dy, h->stats_A, h->Uf[0], h->Uf[1],
+                                                               h->Uf[2], h->sums);
+    else
+        k_stats<double><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->cfg.dy, h->stats_A, h->U[0], h->U[1], h->U[2],
+                                                                h->sums);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -730,8 +865,12 @@ int launch_rescale(tbl_handle* h) {
     int n = (g.ny - 2) * (g.nz - 2);
     int nb = (n + 255) / 256;
     if (nb < 64) nb = 64;
-    k_rescale_tail<<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2,
-                                              h->wsum2, h->ufl_live, h->sums);
+    if (mixed(h))
+        k_rescale_tail<float><<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2,
+                                                         h->vsum2, h->wsum2, h->ufl_live, h->sums);
+    else
+        k_rescale_tail<double><<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->U[0], h->U[1], h->U[2], h->usum2,
+                                                          h->vsum2, h->wsum2, h->ufl_live, h->sums);
     h->launches += 2;
     return TBL_OK;
 }

@@ -33,6 +33,7 @@ namespace tbl {
 
 enum SweepMode { SW_GS = 0, SW_FWD = 1, SW_BWD = 2 };
 
+template <typename T>
 struct SweepArgs {
     Geom g;
     const SweepCta* ctas;
@@ -45,17 +46,17 @@ struct SweepArgs {
     double aw, as;              // 1/dx^2, 1/dy^2
     // GS
     double t;                   // -dt/Re
-    double* F[3];
-    const double* Q[3];
+    T* F[3];
+    const T* Q[3];
     int comp[3];
-    const double* halo_in;      // [comp][side][slab] planes
-    double* halo_out;
+    const T* halo_in;           // [comp][side][slab] planes
+    T* halo_out;
     // SSOR
     double omega, sw;           // w, (2-w)/w
-    const double* X;            // matvec input (FWD) / PCorr (FWD residual mode)
+    const T* X;                 // matvec input (FWD) / PCorr (FWD residual mode)
     const double* Q8;           // residual mode when non-null
-    double* RH;                 // FWD output (unscaled) / BWD input
-    double* OUT;                // BWD output
+    T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
+    T* OUT;                     // BWD output
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
@@ -93,270 +94,350 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
     return true;
 }
 
+constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
+constexpr int PUB = 4;   // global progress is published every PUB steps (and at the end)
+
+__device__ __forceinline__ int ld_acquire_cta(const int* p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cta(int* p, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+
+// Wait until the shared progress word reaches target (false on timeout).
+__device__ __forceinline__ bool wait_cta(const int* p, int target) {
+    long long spins = 0;
+    while (ld_acquire_cta(p) < target) {
+        if (++spins > SPIN_LIMIT) return false;
+        if (spins > 1024) __nanosleep(32);
+    }
+    return true;
+}
+
 // Every warp is an independent unit of the dataflow: it waits only for the
 // warps that produce its (j-1) and (k-1) inputs and publishes its own
-// progress after each step (shared memory for the next plane in the CTA,
-// a global flag for the CTAs downstream).  No CTA-wide barrier in the loop.
-template <int MODE>
-__global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs a) {
+// progress (shared memory every step for the next plane in the CTA, a global
+// flag every PUB steps for the CTAs downstream).  No CTA-wide barrier.
+//
+// Per step a lane updates CH points of its line.  The point update is
+// reassociated so that only one FMA depends on the previous point:
+//   GS : x = rd*Q - rd*cE*U(i+1) - rd*cN*U(j+1) - rd*cT*U(k+1)       (prefetch)
+//            - rd*cS*x(j-1) - rd*cB*x(k-1)                            (after wait)
+//            - rd*cW*x(i-1)                                           (chain)
+//   FWD: x = w'*r + w'*As*x(j-1) + w'*Ab*x(k-1) + w'*Aw*x(i-1),   w' = -w/Ap
+//   BWD: y = w'*s*rhat + w'*As*y(j+1) + w'*At*y(k+1) + w'*Aw*y(i+1)
+// which changes only the rounding of the reference's left-to-right sums.
+// Operands of step T+1 that do not depend on other lines are loaded while
+// step T runs; the (k-1) values of the plane below come through a shared
+// memory ring (RING steps deep, with back-pressure), the (j-1) values of the
+// row above by shuffle or, for lane 0, from global memory.
+template <int MODE, typename Val>
+__global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
+    constexpr int CH = 32 / sizeof(Val);  // points per lane per step: one 32-byte sector
     const Geom& g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const SweepCta cta = a.ctas[blockIdx.x];
     const SlabDesc sl = a.slabs[cta.slab];
-    const int J = g.ny - 2, K = sl.K, C = a.C;
+    const int J = g.ny - 2, K = sl.K;
+    const int C = (g.nx - 2) / CH + 1;     // chunks per line
     const int compi = blockIdx.y;
     const int comp = MODE == SW_GS ? a.comp[compi] : 0;
     unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
-    __shared__ volatile int s_prog[KG];
+    __shared__ int s_prog[KG];
+    __shared__ __align__(16) Val s_ring[KG][RING][32][CH];
     if (lane == 0) s_prog[wid] = -1;
     __syncthreads();
 
-    // logical line coordinates
     const int jl = 32 * cta.jb + lane;  // logical row
     const int kl = KG * cta.kg + wid;   // logical plane
     if (kl >= K) return;                // no lines: nobody waits for this warp
     const bool line_ok = jl < J;
-    // physical coordinates (mirrored for the backward sweep)
     const int jidx = MODE == SW_BWD ? J - 1 - jl : jl;
     const int kidx = MODE == SW_BWD ? K - 1 - kl : kl;
-    const int j = 1 + jidx, k = sl.bn + kidx;
+    const int j = 1 + max(0, min(jidx, J - 1)), k = sl.bn + kidx;
     const int jm = (j == 1) ? g.ny - 2 : j - 1;
     const int jp = (j == g.ny - 2) ? 1 : j + 1;
     const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
+    const long long sy = g.sx;
 
-    // this warp's step range and its upstream warps
     const int jl_last = min(32 * cta.jb + 31, J - 1);
     const int T0 = 32 * cta.jb + kl;
     const int T1 = jl_last + kl + C - 1;
-    const int tend_k = jl_last + kl - 1 + C - 1;  // last step of the (k-1) upstream warp
+    const int tend_k = T1 - 1;          // last step of the (k-1) upstream warp
+    const int tend_j = 32 * cta.jb - 1 + kl + C - 1;
+    const bool has_down = wid < KG - 1 && kl + 1 < K;
     const unsigned long long* fj = cta.up_j >= 0 ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
     const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
     unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
     const unsigned long long tag = a.epoch << 20;
 
-    // per-plane coefficients
-    double cW = 0, cE = 0, cS = 0, cN = 0, cB = 0, cT = 0, rd = 0, wr = 0, sk = 0, ab = 0, at = 0, ap = 0;
+    // coefficients of this plane, pre-scaled for the reassociated update (FP64)
+    double c0 = 0, c1 = 0, c2 = 0, c3 = 0, cjd = 0, ckd = 0, cid = 0;
     if (MODE == SW_GS) {
-        cE = a.t * a.aw; cW = cE; cN = a.t * a.as; cS = cN;
-        cT = a.t * a.At[k]; cB = a.t * a.Ab[k];
-        rd = 1.0 / (1.0 + (a.t * a.Ap[k]));
+        const double rd = 1.0 / (1.0 + (a.t * a.Ap[k]));
+        c0 = rd;                       // * Q
+        c1 = -(a.t * a.aw) * rd;       // * U(i+1)
+        c2 = -(a.t * a.as) * rd;       // * U(j+1)
+        c3 = -(a.t * a.At[k]) * rd;    // * U(k+1)
+        cjd = -(a.t * a.as) * rd;      // * x(j-1)
+        ckd = -(a.t * a.Ab[k]) * rd;   // * x(k-1)
+        cid = -(a.t * a.aw) * rd;      // * x(i-1)
     } else {
-        wr = -a.omega * a.rAp[k];  // -w * rAnp
-        sk = a.sw * a.Ap[k];       // ((2-w)/w) * Anp
-        ab = a.Ab[k]; at = a.At[k]; ap = a.Ap[k];
+        const double wr = -a.omega * a.rAp[k];  // -w * rAnp
+        c0 = MODE == SW_FWD ? wr : wr * (a.sw * a.Ap[k]);
+        cjd = wr * a.as;
+        ckd = wr * (MODE == SW_FWD ? a.Ab[k] : a.At[k]);
+        cid = wr * a.aw;
     }
-    double* F = MODE == SW_GS ? a.F[comp] : nullptr;
-    const double* Qc = MODE == SW_GS ? a.Q[comp] : nullptr;
-    const size_t hplane = (size_t)g.ps;
-    const double* halo_lo = nullptr;
-    const double* halo_hi = nullptr;
-    if (MODE == SW_GS) {
-        const size_t base = (size_t)comp * 2 * a.P;
-        halo_lo = a.halo_in + (base + 0 * a.P + cta.slab) * hplane;
-        halo_hi = a.halo_in + (base + 1 * a.P + cta.slab) * hplane;
-    }
+    const Val p0 = (Val)c0, p1 = (Val)c1, p2 = (Val)c2, p3 = (Val)c3, cj = (Val)cjd, ck = (Val)ckd, ci = (Val)cid;
 
-    double last[CHUNK];  // values this lane produced at the previous step
-    double carry = 0.0;  // logical previous point on the own line
+    // line pointers (physical chunk c at element CH*c)
+    Val* F = MODE == SW_GS ? a.F[comp] + line : nullptr;
+    const Val* Qc = MODE == SW_GS ? a.Q[comp] + line : nullptr;
+    const Val* Fjp = MODE == SW_GS ? a.F[comp] + sy * ((long long)jp + (long long)g.ny * k) : nullptr;
+    const Val* Fkp = nullptr;
+    const Val* kin = nullptr;  // plane below (global): warp 0 across CTAs, slab edge
+    const Val* jin = nullptr;  // row above (global): lane 0
+    bool kin_zero = false, jin_zero = false;
+    Val* hout = nullptr;  // GS: next sweep's halo copy of this plane
+    if (MODE == SW_GS) {
+        const size_t hp = (size_t)g.ps, base = (size_t)comp * 2 * a.P;
+        Fkp = (kidx == K - 1 && cta.slab < a.P - 1) ? a.halo_in + (base + 1 * a.P + cta.slab) * hp + sy * j
+                                                    : a.F[comp] + line + g.ps;
+        kin = (kidx == 0 && cta.slab > 0) ? a.halo_in + (base + 0 * a.P + cta.slab) * hp + sy * j
+                                          : a.F[comp] + line - g.ps;
+        jin = a.F[comp] + sy * ((long long)jm + (long long)g.ny * k);
+        if (kidx == 0 && cta.slab > 0) hout = a.halo_out + (base + 1 * a.P + (cta.slab - 1)) * hp + sy * j;
+        if (kidx == K - 1 && cta.slab < a.P - 1) hout = a.halo_out + (base + 0 * a.P + (cta.slab + 1)) * hp + sy * j;
+    } else {
+        Val* io = MODE == SW_FWD ? a.RH : a.OUT;
+        kin_zero = MODE == SW_FWD ? (kidx == 0) : (kidx == K - 1);
+        kin = io + line + (MODE == SW_FWD ? -g.ps : g.ps);
+        jin_zero = MODE == SW_FWD ? (jidx == 0) : (jidx == J - 1);
+        jin = io + sy * ((long long)(jin_zero ? j : (MODE == SW_FWD ? j - 1 : j + 1)) + (long long)g.ny * k);
+    }
+    Val* outp = MODE == SW_GS ? F : (MODE == SW_FWD ? a.RH : a.OUT) + line;
+    const Val* inp = MODE == SW_GS ? nullptr : a.RH + line;
+    const bool wrap = MODE == SW_GS && jp == 1;  // the row after j holds new values (periodic GS)
+
+    Val last[CH];
 #pragma unroll
-    for (int e = 0; e < CHUNK; ++e) last[e] = 0.0;
-    long long seen_j = -1, seen_k = -1;  // upstream progress known to lane 0
+    for (int e = 0; e < CH; ++e) last[e] = Val(0);
+    Val carry = Val(0);
+    long long seen_j = -1, seen_k = -1;
+
+    // raw operands loaded one step ahead
+    Val ra[CH], rb[CH], rc[CH], rd_[CH];
+    Val rnx = Val(0);
+    auto load_raw = [&](int ts) {
+        const int cl = ts - jl - kl;
+        if (!line_ok || cl < 0 || cl >= C) return;
+        const int i0 = CH * (MODE == SW_BWD ? C - 1 - cl : cl);
+        if (MODE == SW_GS) {
+#pragma unroll
+            for (int e = 0; e < CH; ++e) { ra[e] = Qc[i0 + e]; rb[e] = F[i0 + e]; }
+            rnx = (i0 + CH - 1 <= g.nx - 2) ? F[i0 + CH] : Val(0);
+            if (!wrap) {
+#pragma unroll
+                for (int e = 0; e < CH; ++e) rc[e] = __ldcg(Fjp + i0 + e);
+            }
+#pragma unroll
+            for (int e = 0; e < CH; ++e) rd_[e] = __ldcg(Fkp + i0 + e);
+        } else {
+#pragma unroll
+            for (int e = 0; e < CH; ++e) ra[e] = inp[i0 + e];
+        }
+    };
+    Val pre[CH];
+    auto make_pre = [&](int ts) {
+        const int cl = ts - jl - kl;
+        if (!line_ok || cl < 0 || cl >= C) return;
+        if (MODE == SW_GS) {
+#pragma unroll
+            for (int e = 0; e < CH; ++e) {
+                Val oip = e < CH - 1 ? rb[e + 1] : rnx;
+                Val x = fma(p1, oip, p0 * ra[e]);
+                if (!wrap) x = fma(p2, rc[e], x);
+                pre[e] = fma(p3, rd_[e], x);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < CH; ++e) pre[e] = p0 * ra[e];
+        }
+    };
+    load_raw(T0);
+    make_pre(T0);
+    Val bnd = MODE == SW_GS ? rb[0] : Val(0);  // GS: U(0) of the first chunk
+    Val pj_pf[CH], pk_pf[CH];
+    bool pj_ok = false, pk_ok = false;
+    int abort = 0;
 
     for (int T = T0; T <= T1; ++T) {
-        const int cl = T - jl - kl;  // logical chunk of this lane
+        const int cl = T - jl - kl;
         const bool act = line_ok && cl >= 0 && cl < C;
-        const int c = MODE == SW_BWD ? C - 1 - cl : cl;  // physical chunk
-        const int i0 = 4 * c;
-        // ---- operands that do not depend on this step's predecessors
-        double rhs[CHUNK], oi[CHUNK], ojp[CHUNK], okp[CHUNK];
-        double nxt = 0.0;
-        if (act) {
-            if (MODE == SW_GS) {
-                const double* Fl = F + line + i0;
-                const double* Ql = Qc + line + i0;
+        const int c = MODE == SW_BWD ? C - 1 - cl : cl;
+        const int i0 = CH * c;
+        const bool edge = (c == 0) || (c == C - 1);
+        Val cur[CH];
 #pragma unroll
-                for (int e = 0; e < CHUNK; ++e) { oi[e] = Fl[e]; rhs[e] = Ql[e]; }
-                if (i0 + 3 <= g.nx - 2) nxt = Fl[4];
-                if (jp != 1) {  // the wrapped row holds new values: read after the wait
-                    const double* Fj = F + (long long)g.sx * ((long long)jp + (long long)g.ny * k) + i0;
-#pragma unroll
-                    for (int e = 0; e < CHUNK; ++e) ojp[e] = __ldcg(Fj + e);
-                }
-                const double* Fk = (kidx == K - 1 && cta.slab < a.P - 1) ? halo_hi + (long long)g.sx * j + i0
-                                                                         : F + line + g.ps + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) okp[e] = __ldcg(Fk + e);
-            } else if (MODE == SW_FWD) {
-                // r = L7 X (matvec) or Q8 - L7 X (restart residual), global halos
-                const double* Xl = a.X + line + i0;
-                const double* Xjm = a.X + (long long)g.sx * ((long long)jm + (long long)g.ny * k) + i0;
-                const double* Xjp = a.X + (long long)g.sx * ((long long)jp + (long long)g.ny * k) + i0;
-                const double* Xkm = Xl - g.ps;
-                const double* Xkp = Xl + g.ps;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) {
-                    const int i = i0 + e;
-                    rhs[e] = 0.0;
-                    if (i >= 1 && i <= g.nx - 2) {
-                        double lap = a.aw * Xl[e - 1] + a.aw * Xl[e + 1] + a.as * Xjm[e] + a.as * Xjp[e] +
-                                     ab * Xkm[e] + at * Xkp[e] + ap * Xl[e];
-                        rhs[e] = a.Q8 ? (a.Q8[line + i0 + e] - (lap)) : lap;
-                    }
-                }
-            } else {
-                const double* Rl = a.RH + line + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) rhs[e] = sk * Rl[e];
-            }
-        }
-        // ---- wait for the producers of step T-1 (lane 0 polls for the warp)
-        const int cl0 = T - 32 * cta.jb - kl;           // lane 0's chunk
-        const bool lane0_act = cl0 >= 0 && cl0 < C;
-        const bool any_act = cl0 >= 0 && (T - jl_last - kl) < C;
-        int abort = 0;
-        if (lane == 0 && any_act) {
-            if (fj && lane0_act && seen_j < T - 1) {
+        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
+        const Val cbnd = bnd;
+        load_raw(T + 1);
+        // ---- wait for the producers of step T-1 (lane 0 for the warp)
+        if (lane == 0) {
+            const int cl0 = T - 32 * cta.jb - kl;
+            if (fj && cl0 >= 0 && cl0 < C && !pj_ok && seen_j < T - 1) {
                 seen_j = wait_global(fj, tag, T - 1);
                 if (seen_j < 0) abort = 1;
             }
-            if (!abort && kl > 0) {
+            if (kl > 0 && cl0 >= 0 && T - jl_last - kl < C) {
                 const int target = min(T - 1, tend_k);
                 if (wid > 0) {
-                    if (!wait_shared(&s_prog[wid - 1], target)) abort = 1;
-                } else if (fk && seen_k < target) {
+                    if (!wait_cta(&s_prog[wid - 1], target)) abort = 1;
+                } else if (fk && !pk_ok && seen_k < target) {
                     seen_k = wait_global(fk, tag, target);
                     if (seen_k < 0) abort = 1;
                 }
             }
-            if (abort) atomicExch(a.err, TBL_ERR_TIMEOUT);
         }
-        abort = __shfl_sync(0xffffffffu, abort, 0);
-        if (abort) return;
         __syncwarp();
-        // ---- predecessor values: (j-1) by shuffle or global, (k-1) through memory
-        double pj[CHUNK], pk[CHUNK];
+        // ---- predecessors
+        Val pj[CH], pk[CH];
 #pragma unroll
-        for (int e = 0; e < CHUNK; ++e) pj[e] = __shfl_up_sync(0xffffffffu, last[e], 1);
-        if (act) {
-            if (MODE == SW_GS && jp == 1) {
-                const double* Fj = F + (long long)g.sx * ((long long)jp + (long long)g.ny * k) + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) ojp[e] = __ldcg(Fj + e);
-            }
-            if (lane == 0) {
-                if (MODE == SW_GS) {  // row j-1 (wrapped: old value of the last row for j=1)
-                    const double* s = F + (long long)g.sx * ((long long)jm + (long long)g.ny * k) + i0;
-#pragma unroll
-                    for (int e = 0; e < CHUNK; ++e) pj[e] = __ldcg(s + e);
-                } else {
-                    const bool edge = MODE == SW_FWD ? (jidx == 0) : (jidx == J - 1);
-                    const double* base = MODE == SW_FWD ? a.RH : a.OUT;
-                    const int jn = MODE == SW_FWD ? j - 1 : j + 1;
-                    const double* s = base + (long long)g.sx * ((long long)jn + (long long)g.ny * k) + i0;
-#pragma unroll
-                    for (int e = 0; e < CHUNK; ++e) pj[e] = edge ? 0.0 : __ldcg(s + e);
-                }
-            }
-            if (MODE == SW_GS) {
-                const double* s = (kidx == 0 && cta.slab > 0) ? halo_lo + (long long)g.sx * j + i0
-                                                              : F + line - g.ps + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) pk[e] = __ldcg(s + e);
-            } else {
-                const bool edge = MODE == SW_FWD ? (kidx == 0) : (kidx == K - 1);
-                const double* base = MODE == SW_FWD ? a.RH : a.OUT;
-                const double* s = base + line + (MODE == SW_FWD ? -g.ps : g.ps) + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) pk[e] = edge ? 0.0 : __ldcg(s + e);
-            }
-            // ---- the chunk, sequential along the line
-            double nv[CHUNK];
-            if (MODE == SW_GS) {
-                double prev = (c == 0) ? oi[0] : carry;  // i=0 is the inflow boundary value
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) {
-                    const int i = i0 + e;
-                    if (i >= 1 && i <= g.nx - 2) {
-                        double oip = e < CHUNK - 1 ? oi[e + 1] : nxt;
-                        double x = rhs[e] - cE * oip - cW * prev - cN * ojp[e] - cS * pj[e] - cT * okp[e] - cB * pk[e];
-                        x = x * rd;
-                        nv[e] = x;
-                        prev = x;
-                    } else {
-                        nv[e] = oi[e];
-                        prev = oi[e];
-                    }
-                }
-                carry = prev;
-                double* Fl = F + line + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) {
-                    const int i = i0 + e;
-                    if (i >= 1 && i <= g.nx - 2) Fl[e] = nv[e];
-                }
-                // next sweep's halo planes of the neighbouring slabs
-                if (kidx == 0 && cta.slab > 0) {
-                    double* hd = a.halo_out + ((size_t)comp * 2 * a.P + 1 * a.P + (cta.slab - 1)) * hplane +
-                                 (long long)g.sx * j + i0;
-#pragma unroll
-                    for (int e = 0; e < CHUNK; ++e)
-                        if (i0 + e >= 1 && i0 + e <= g.nx - 2) hd[e] = nv[e];
-                }
-                if (kidx == K - 1 && cta.slab < a.P - 1) {
-                    double* hd = a.halo_out + ((size_t)comp * 2 * a.P + 0 * a.P + (cta.slab + 1)) * hplane +
-                                 (long long)g.sx * j + i0;
-#pragma unroll
-                    for (int e = 0; e < CHUNK; ++e)
-                        if (i0 + e >= 1 && i0 + e <= g.nx - 2) hd[e] = nv[e];
-                }
-            } else if (MODE == SW_FWD) {
-                double prev = (c == 0) ? 0.0 : carry;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) {
-                    const int i = i0 + e;
-                    if (i >= 1 && i <= g.nx - 2) {
-                        double x = (rhs[e] + a.aw * prev + a.as * pj[e] + ab * pk[e]) * wr;
-                        nv[e] = x;
-                        prev = x;
-                    } else {
-                        nv[e] = 0.0;
-                        prev = 0.0;
-                    }
-                }
-                carry = prev;
-                double* Rl = a.RH + line + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) Rl[e] = nv[e];
-            } else {  // SW_BWD: descending i inside the chunk
-                double prev = (c == C - 1) ? 0.0 : carry;
-#pragma unroll
-                for (int e = CHUNK - 1; e >= 0; --e) {
-                    const int i = i0 + e;
-                    if (i >= 1 && i <= g.nx - 2) {
-                        double y = (rhs[e] + a.aw * prev + a.as * pj[e] + at * pk[e]) * wr;
-                        nv[e] = y;
-                        prev = y;
-                    } else {
-                        nv[e] = 0.0;
-                        prev = 0.0;
-                    }
-                }
-                carry = prev;
-                double* Ol = a.OUT + line + i0;
-#pragma unroll
-                for (int e = 0; e < CHUNK; ++e) Ol[e] = nv[e];
-            }
-#pragma unroll
-            for (int e = 0; e < CHUNK; ++e) last[e] = nv[e];
+        for (int e = 0; e < CH; ++e) pj[e] = __shfl_up_sync(0xffffffffu, last[e], 1);
+        if (__shfl_sync(0xffffffffu, abort, 0)) {
+            if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
+            return;
         }
-        // ---- publish step T: the next plane of this CTA, then the CTAs downstream
+        if (act) {
+            if (lane == 0) {
+#pragma unroll
+                for (int e = 0; e < CH; ++e) pj[e] = pj_ok ? pj_pf[e] : (jin_zero ? Val(0) : __ldcg(jin + i0 + e));
+            }
+            if (wid > 0) {
+                const Val* rs = &s_ring[wid - 1][(T - 1) & (RING - 1)][lane][0];
+#pragma unroll
+                for (int e = 0; e < CH; ++e) pk[e] = rs[e];
+            } else {
+#pragma unroll
+                for (int e = 0; e < CH; ++e) pk[e] = pk_ok ? pk_pf[e] : (kin_zero ? Val(0) : __ldcg(kin + i0 + e));
+            }
+            if (wrap) {
+#pragma unroll
+                for (int e = 0; e < CH; ++e) cur[e] = fma(p2, __ldcg(Fjp + i0 + e), cur[e]);
+            }
+            Val nv[CH];
+#pragma unroll
+            for (int e = 0; e < CH; ++e) nv[e] = fma(cj, pj[e], fma(ck, pk[e], cur[e]));
+            if (!edge) {
+                if (MODE != SW_BWD) {
+#pragma unroll
+                    for (int e = 0; e < CH; ++e) { carry = fma(ci, carry, nv[e]); nv[e] = carry; }
+                } else {
+#pragma unroll
+                    for (int e = CH - 1; e >= 0; --e) { carry = fma(ci, carry, nv[e]); nv[e] = carry; }
+                }
+#pragma unroll
+                for (int e = 0; e < CH; ++e) outp[i0 + e] = nv[e];
+                if (MODE == SW_GS && hout) {
+#pragma unroll
+                    for (int e = 0; e < CH; ++e) hout[i0 + e] = nv[e];
+                }
+            } else {  // first / last chunk: points outside 1..nx-2 are boundary values or zero
+                if (MODE != SW_BWD) {
+                    Val prev = c == 0 ? (MODE == SW_GS ? cbnd : Val(0)) : carry;
+#pragma unroll
+                    for (int e = 0; e < CH; ++e) {
+                        const int i = i0 + e;
+                        if (i >= 1 && i <= g.nx - 2) { prev = fma(ci, prev, nv[e]); nv[e] = prev; }
+                        else { nv[e] = (MODE == SW_GS && i == 0) ? cbnd : Val(0); prev = nv[e]; }
+                    }
+                    carry = prev;
+                } else {
+                    Val prev = c == C - 1 ? Val(0) : carry;
+#pragma unroll
+                    for (int e = CH - 1; e >= 0; --e) {
+                        const int i = i0 + e;
+                        if (i >= 1 && i <= g.nx - 2) { prev = fma(ci, prev, nv[e]); nv[e] = prev; }
+                        else { nv[e] = Val(0); prev = Val(0); }
+                    }
+                    carry = prev;
+                }
+#pragma unroll
+                for (int e = 0; e < CH; ++e) {
+                    const int i = i0 + e;
+                    if (MODE != SW_GS || (i >= 1 && i <= g.nx - 2)) outp[i0 + e] = nv[e];
+                    if (MODE == SW_GS && hout && i >= 1 && i <= g.nx - 2) hout[i0 + e] = nv[e];
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < CH; ++e) last[e] = nv[e];
+        }
+        // ---- hand the chunk to the next plane (ring slot T % RING), publish
+        if (has_down) {
+            if (lane == 0 && T - RING + 1 >= T0 + 1)
+                if (!wait_cta(&s_prog[wid + 1], min(T - RING + 1, T1 + 1))) abort = 1;
+            __syncwarp();
+            if (__shfl_sync(0xffffffffu, abort, 0)) {
+                if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
+                return;
+            }
+            Val* ws = &s_ring[wid][T & (RING - 1)][lane][0];
+#pragma unroll
+            for (int e = 0; e < CH; ++e) ws[e] = last[e];
+        }
         __syncwarp();
         if (lane == 0) {
-            __threadfence_block();
-            s_prog[wid] = T;
-            st_release(fme, tag + (unsigned long long)(T + 1));
+            st_release_cta(&s_prog[wid], T);
+            if ((T - T0) % PUB == PUB - 1 || T == T1) st_release(fme, tag + (unsigned long long)(T + 1));
         }
+        // ---- cross-CTA inputs of step T+1 when their producer is known to be ahead
+        pj_ok = false;
+        pk_ok = false;
+        if (T < T1) {
+            const int cln = T + 1 - jl - kl;
+            const bool actn = line_ok && cln >= 0 && cln < C;
+            const int i0n = CH * (MODE == SW_BWD ? C - 1 - cln : cln);
+            if (lane == 0 && fj && seen_j >= T && actn) {
+#pragma unroll
+                for (int e = 0; e < CH; ++e) pj_pf[e] = jin_zero ? Val(0) : __ldcg(jin + i0n + e);
+                pj_ok = true;
+            }
+            if (wid == 0 && fk) {
+                const int pf = __shfl_sync(0xffffffffu, (lane == 0 && seen_k >= min(T, tend_k)) ? 1 : 0, 0);
+                if (pf && actn) {
+#pragma unroll
+                    for (int e = 0; e < CH; ++e) pk_pf[e] = kin_zero ? Val(0) : __ldcg(kin + i0n + e);
+                }
+                pk_ok = pf != 0;
+            }
+        }
+        make_pre(T + 1);
+        if (MODE == SW_GS) bnd = rb[0];
     }
+    (void)tend_j;
+}
+
+// r = L7 X (Q8 == nullptr) or r = Q8 - L7 X on the interior, written to R
+// (:1001-1006 restart residual, :1098-1101 Arnoldi matvec), global halos.
+template <typename TI, typename TO, typename TC>
+__global__ void __launch_bounds__(256) k_lap(Geom g, double aw_, double as_, const double* __restrict__ Ab,
+                                             const double* __restrict__ At, const double* __restrict__ Ap,
+                                             const TI* __restrict__ X, const double* __restrict__ Q8,
+                                             TO* __restrict__ R) {
+    const TC aw = (TC)aw_, as = (TC)as_;
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    if (i > g.nx - 2) return;
+    const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
+    const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
+    const TC xjm = (TC)X[(long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k)];
+    const TC xjp = (TC)X[(long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k)];
+    TC lap = aw * (TC)X[p - 1] + aw * (TC)X[p + 1] + as * xjm + as * xjp + (TC)Ab[k] * (TC)X[p - g.ps] +
+             (TC)At[k] * (TC)X[p + g.ps] + (TC)Ap[k] * (TC)X[p];
+    R[p] = (TO)(Q8 ? ((TC)Q8[p] - (lap)) : lap);
 }
 
 // ------------------------------------------------------------- host glue
@@ -392,8 +473,9 @@ int build_sweep_ctas(tbl_handle* h) {
     return TBL_OK;
 }
 
-static SweepArgs base_args(tbl_handle* h) {
-    SweepArgs a;
+template <typename T>
+static SweepArgs<T> base_args(tbl_handle* h) {
+    SweepArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.g = h->g;
     a.ctas = h->ctas;
@@ -413,63 +495,102 @@ static SweepArgs base_args(tbl_handle* h) {
     return a;
 }
 
-template <int MODE>
-static int launch_sweep(tbl_handle* h, SweepArgs& a, int ncomp) {
+template <int MODE, typename T>
+static int launch_sweep(tbl_handle* h, SweepArgs<T>& a, int ncomp) {
     void* args[] = {&a};
     dim3 grid(h->n_cta, ncomp), block(KG * 32);
-    TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE>, grid, block, args, 0, h->stream));
+    TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE, T>, grid, block, args, 0, h->stream));
     h->launches++;
     return TBL_OK;
 }
 
 // GS sweep for the listed components; halo buffers ping-pong by `parity`.
 int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity) {
-    SweepArgs a = base_args(h);
+    const size_t hsz = (size_t)3 * 2 * h->P * h->g.ps;
+    if (h->cfg.precision == TBL_PREC_MIXED) {  // delta form: iterate on D with r0 in Qf
+        SweepArgs<float> a = base_args<float>(h);
+        for (int c = 0; c < 3; ++c) { a.F[c] = h->Df[c]; a.Q[c] = h->Qf[c]; }
+        for (int c = 0; c < ncomp; ++c) a.comp[c] = comps[c];
+        float* hf = reinterpret_cast<float*>(h->halo);
+        a.halo_in = hf + (size_t)(parity & 1) * hsz;
+        a.halo_out = hf + (size_t)((parity + 1) & 1) * hsz;
+        return launch_sweep<SW_GS, float>(h, a, ncomp);
+    }
+    SweepArgs<double> a = base_args<double>(h);
     for (int c = 0; c < 3; ++c) { a.F[c] = h->U[c]; a.Q[c] = h->Q[c]; }
     for (int c = 0; c < ncomp; ++c) a.comp[c] = comps[c];
-    const size_t hsz = (size_t)3 * 2 * h->P * h->g.ps;
     a.halo_in = h->halo + (size_t)(parity & 1) * hsz;
     a.halo_out = h->halo + (size_t)((parity + 1) & 1) * hsz;
-    return launch_sweep<SW_GS>(h, a, ncomp);
+    return launch_sweep<SW_GS, double>(h, a, ncomp);
 }
 
 // Forward SSOR sweep of r = L7 X (Q8 == nullptr) or r = Q8 - L7 X.
 int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
-    SweepArgs a = base_args(h);
-    a.X = X;
-    a.Q8 = Q8;
+    const Geom& g = h->g;
+    k_lap<double, double, double><<<dim3((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2), 256, 0, h->stream>>>(
+        g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH);
+    h->launches++;
+    SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
-    return launch_sweep<SW_FWD>(h, a, 1);
+    return launch_sweep<SW_FWD, double>(h, a, 1);
 }
 
 int launch_ssor_bwd(tbl_handle* h, double* out) {
-    SweepArgs a = base_args(h);
+    SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     a.OUT = out;
-    return launch_sweep<SW_BWD>(h, a, 1);
+    return launch_sweep<SW_BWD, double>(h, a, 1);
+}
+
+// Mixed precision: FP32 preconditioned matvec of the inner GMRES.  Xd (FP64
+// outer residual, r = Q8 - L7 p' computed in FP64) or Xf (inner FP32 vector).
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8) {
+    const Geom& g = h->g;
+    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
+    const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
+    if (PCd)
+        k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf);
+    else
+        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, Xf, nullptr, h->RHf);
+    h->launches++;
+    SweepArgs<float> a = base_args<float>(h);
+    a.RH = h->RHf;
+    return launch_sweep<SW_FWD, float>(h, a, 1);
+}
+
+int launch_ssor_bwd_f(tbl_handle* h, float* out) {
+    SweepArgs<float> a = base_args<float>(h);
+    a.RH = h->RHf;
+    a.OUT = out;
+    return launch_sweep<SW_BWD, float>(h, a, 1);
 }
 
 // Snapshot of the planes every slab reads from its neighbours before the
 // first sweep (the end-of-step halo of the previous step).
-__global__ void k_halo_init(Geom g, const SlabDesc* __restrict__ slabs, int P, const double* __restrict__ U0,
-                            const double* __restrict__ U1, const double* __restrict__ U2, double* __restrict__ halo) {
+template <typename T>
+__global__ void k_halo_init(Geom g, const SlabDesc* __restrict__ slabs, int P, const T* __restrict__ U0,
+                            const T* __restrict__ U1, const T* __restrict__ U2, T* __restrict__ halo) {
     // blockIdx.y = comp*2P + side*P + slab
     const int comp = blockIdx.y / (2 * P), rem = blockIdx.y % (2 * P), side = rem / P, r = rem % P;
     const SlabDesc s = slabs[r];
     if (side == 0 && r == 0) return;
     if (side == 1 && r == P - 1) return;
     const int kk = side == 0 ? s.bn - 1 : s.bn + s.K;
-    const double* F = comp == 0 ? U0 : (comp == 1 ? U1 : U2);
-    double* dst = halo + (size_t)blockIdx.y * g.ps;
-    const double* src = F + (long long)kk * g.ps;
+    const T* F = comp == 0 ? U0 : (comp == 1 ? U1 : U2);
+    T* dst = halo + (size_t)blockIdx.y * g.ps;
+    const T* src = F + (long long)kk * g.ps;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < g.ps; q += (long long)gridDim.x * blockDim.x)
         dst[q] = src[q];
 }
 
 int launch_halo_init(tbl_handle* h, int parity) {
     const size_t hsz = (size_t)3 * 2 * h->P * h->g.ps;
-    k_halo_init<<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(h->g, h->slabs, h->P, h->U[0], h->U[1], h->U[2],
-                                                               h->halo + (size_t)(parity & 1) * hsz);
+    if (h->cfg.precision == TBL_PREC_MIXED)
+        k_halo_init<float><<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(
+            h->g, h->slabs, h->P, h->Df[0], h->Df[1], h->Df[2], reinterpret_cast<float*>(h->halo) + (size_t)(parity & 1) * hsz);
+    else
+        k_halo_init<double><<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(h->g, h->slabs, h->P, h->U[0], h->U[1],
+                                                                           h->U[2], h->halo + (size_t)(parity & 1) * hsz);
     h->launches++;
     return TBL_OK;
 }
@@ -480,7 +601,7 @@ int check_cooperative(tbl_handle* h) {
     TBL_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     TBL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int per_sm = 0;
-    TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_sweep<SW_GS>, KG * 32, 0));
+    TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_sweep<SW_GS, double>, KG * 32, 0));
     h->coop_ok = coop && (long long)per_sm * sms >= 3LL * h->n_cta;
     return h->coop_ok ? TBL_OK : TBL_ERR_BAD_ARG;
 }

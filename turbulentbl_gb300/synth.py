@@ -189,7 +189,7 @@ def make_state(wl, nproc=8, rms=0.05, dt=None):
     if dt is None:
         dt = cfl_dt(u, v, w, mesh, wl.cfl)
     rp = RunParams(dt=dt, re=re, ue=ue, nproc=nproc, irec=irec, kmax=wl.kmax, errtol=wl.errtol,
-                   precision=wl.precision)
+                   precision=wl.precision, mixed_kmax=wl.kmax, mixed_outer_tol=wl.errtol)
     state = dict(u=u, v=v, w=w, p=np.zeros((nx, ny, nz), order="F"), pcorr=np.zeros((nx, ny, nz), order="F"),
                  usum2=usum2, vsum2=vsum2, wsum2=wsum2, wt=np.asfortranarray(wt), uf=uf, vf=vf, wf=wf,
                  newk=newk, ume1=ume1.copy(), bltkns=bl, lamda=1.0, time=0.0, nstep=0, cont=0, ksep=ksep)
