@@ -15,6 +15,8 @@ def lib():
         _lib = C.CDLL(_build.build())
         _lib.orc_apply_lap.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.orc_apply_ssor.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.orc_solve_ppe.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int32)]
     return _lib
 
 
@@ -27,6 +29,14 @@ class OracleRunner(AbiRunner):
         y = np.zeros_like(x, order="F")
         lib().orc_apply_lap(self._h, x.ctypes.data_as(C.POINTER(C.c_double)), y.ctypes.data_as(C.POINTER(C.c_double)))
         return y
+
+    def solve_ppe(self, rhs):
+        rhs = np.asfortranarray(rhs, dtype=np.float64)
+        x = np.zeros_like(rhs, order="F")
+        it = C.c_int32(0)
+        st = lib().orc_solve_ppe(self._h, rhs.ctypes.data_as(C.POINTER(C.c_double)),
+                                 x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it))
+        return st, x, it.value
 
     def apply_ssor(self, x):
         x = np.asfortranarray(x, dtype=np.float64)

@@ -1044,6 +1044,23 @@ int orc_apply_lap(orc_handle* h, const double* x, double* y) {
     return TBL_OK;
 }
 
+// Solves L7 x = rhs by the step's GMRES (block-SSOR preconditioned) from
+// x = 0 with the configured kmax / errtol; returns the status and the
+// number of Arnoldi steps.
+int orc_solve_ppe(orc_handle* h, const double* rhs, double* x, int32_t* iters) {
+    if (!h || !rhs || !x) return TBL_ERR_BAD_ARG;
+    Oracle& o = h->o;
+    std::memcpy(o.Q8.data(), rhs, o.N * 8);
+    std::fill(o.PC.begin(), o.PC.end(), 0.0);
+    std::vector<int32_t> kits;
+    int restarts = 0, it = 0;
+    double resid = 0.0;
+    int s = gmres(o, nullptr, kits, restarts, it, resid);
+    std::memcpy(x, o.PC.data(), o.N * 8);
+    if (iters) *iters = it;
+    return s;
+}
+
 // Applies the block-SSOR preconditioner to x (interior), result in y.
 int orc_apply_ssor(orc_handle* h, const double* x, double* y) {
     if (!h) return TBL_ERR_BAD_ARG;
