@@ -199,6 +199,30 @@ int tbl_upload_fields(tbl_handle* h, const double* u, const double* v, const dou
 int tbl_profile(tbl_handle* h, int enable);
 int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches, int ngroups);
 
+/* ---- Allocation-free divergence diagnostic ------------------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory (a host code whose own pool allocator owns
+ * every byte of the GPU, or a time loop in which an allocation could
+ * synchronise the device).  It computes the reference's divergence printout
+ * |sum div U| / ((nx-2)(ny-2)(nz-2)) (the value tbl_step reports as div_diag)
+ * for fields the caller already holds on the current device, and allocates
+ * nothing: its only scratch is a fixed array of TBL_NOALLOC_BLOCKS doubles in
+ * the library image, held by every GPU that loads the library until exit.
+ *   cfg     grid sizes and dx, dy, dxi (other fields unused)
+ *   jacinv  device, nz doubles: 1/Jac(k)
+ *   u,v,w   device, nx*ny*nz doubles each, the reference layout (i fastest)
+ *   out     device, one double receiving the result
+ * Runs asynchronously on the legacy default stream.  The first call on a
+ * device looks up the scratch address (make it before any stream capture).
+ * Calls share the scratch: calls that overlap on the GPU race.  Grids with
+ * more than TBL_NOALLOC_MAX_POINTS interior points are rejected with
+ * TBL_ERR_TOO_LARGE. */
+#define TBL_ERR_TOO_LARGE     -10
+#define TBL_NOALLOC_BLOCKS     4096
+#define TBL_NOALLOC_MAX_POINTS ((int64_t)TBL_NOALLOC_BLOCKS * 256 * 64)
+int tbl_div_diag_noalloc(const tbl_config* cfg, const double* jacinv, const double* u, const double* v,
+                         const double* w, double* out);
+
 /* Release everything. */
 void tbl_destroy(tbl_handle* h);
 

@@ -17,6 +17,7 @@ TBL_ERR_TIMEOUT = -6
 TBL_ERR_NO_DEVICE = -7
 TBL_ERR_REPLAY = -8
 TBL_ERR_ZERO_RHS = -9
+TBL_ERR_TOO_LARGE = -10
 
 STATUS_NAMES = {
     TBL_OK: "OK",
@@ -29,6 +30,7 @@ STATUS_NAMES = {
     TBL_ERR_NO_DEVICE: "NO_DEVICE",
     TBL_ERR_REPLAY: "REPLAY",
     TBL_ERR_ZERO_RHS: "ZERO_RHS",
+    TBL_ERR_TOO_LARGE: "TOO_LARGE",
 }
 
 TBL_PREC_FP64 = 0
