@@ -5,6 +5,7 @@ on the 512 x 128 x 128 seeded box (nx x ny_wall x nz_span; reference arrays
 n3d = (512, 130, 128)), GMRES restart 40, tol 1e-10, P = 8 virtual slabs.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --adjoint [--window 50] [--ckpt 10] [--fd-dirs 4]
 
 One "step" is one full time step of the reference time loop (inflow,
 convection, implicit diffusion, pressure-Poisson GMRES, projection, BCs,
@@ -236,6 +237,50 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     return out
 
 
+def run_adjoint(wl, nproc, window, ckpt, n_fd, local):
+    """Adjoint of a window on the adjoint workload: cost of tbl_backward_window
+    (recomputation from checkpoints + adjoint steps) against tbl_forward_window,
+    and the gradient against central differences of the forward window."""
+    import torch
+    torch.cuda.set_device(local)
+    from turbulentbl_gb300.lib import TblGpu
+    mesh, rp, st = make_state(wl, nproc=nproc)
+    rp.errorstop = 1e-10  # tight implicit-diffusion solves so that differences resolve the gradient
+    rp.cum = 10 ** 6      # no rescaling inside the window
+    g = TblGpu(mesh, rp)
+    g.upload(st)
+    rng = np.random.default_rng(wl.seed)
+    c = rng.normal(0.0, 1e-3, (mesh.nx, mesh.ny - 2))
+    g.set_wall_control(c)
+    g.step(2)
+    x0 = g.download()
+    patch = (10.0, 14.0)
+
+    def fwd(cc):
+        g.upload(x0)
+        g.set_wall_control(cc)
+        J, recs = g.forward_window(window, patch[0], patch[1], ckpt)
+        return J, recs
+
+    fwd(c)  # warm-up (allocates the tape)
+    J, recs = fwd(c)
+    grad, _, ast = g.backward_window(1.0)
+    fd = []
+    for q in range(n_fd):
+        d = rng.normal(0.0, 1e-3, c.shape)
+        eps = 1e-2
+        Jp, _ = fwd(c + eps * d)
+        Jm, _ = fwd(c - eps * d)
+        fdv = (Jp - Jm) / (2 * eps)
+        adv = float((grad * d).sum())
+        fd.append({"fd": fdv, "adjoint": adv, "rel_err": abs(fdv - adv) / abs(adv)})
+    g.close()
+    return {"objective": J, "forward_ms": ast["forward_ms"], "backward_ms": ast["backward_ms"],
+            "ratio": ast["backward_ms"] / ast["forward_ms"], "adjoint_stats": ast, "fd": fd,
+            "gmres_iters_forward": sum(r["gmres_iters"] for r in recs),
+            "gs_sweeps_forward": sum(sum(r["gs_sweeps"]) for r in recs), "grad_norm": float(np.linalg.norm(grad))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -247,8 +292,31 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=30.0, help="seconds of CPU time for the CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time the discrete adjoint of a window on the 256x96x96 adjoint workload instead")
+    ap.add_argument("--window", type=int, default=50)
+    ap.add_argument("--ckpt", type=int, default=10)
+    ap.add_argument("--fd-dirs", type=int, default=4)
     args = ap.parse_args()
     world, rank, local = dist_setup()
+    if args.adjoint:
+        if rank != 0:
+            return
+        wl = WORKLOADS["box256_adjoint"]
+        r = run_adjoint(wl, args.nproc, args.window, args.ckpt, args.fd_dirs, local)
+        line = {"metric": "adjoint/forward cost", "value": r["ratio"], "unit": "x", "n_gpus": 1,
+                "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": wl.name, "reference_n3d": list(wl.n3d), "window_steps": args.window,
+                           "checkpoint_every": args.ckpt, "objective": "mean wall shear, x in [10, 14]",
+                           "control": "wall-normal blowing, nx x (ny-2), N(0, 1e-3)", "gs_errorstop": 1e-10,
+                           "gmres_tol": wl.errtol, "virtual_ranks": args.nproc},
+                "forward_ms": r["forward_ms"], "backward_ms": r["backward_ms"],
+                "objective": r["objective"], "grad_norm": r["grad_norm"],
+                "fd_check": r["fd"], "max_fd_rel_err": max([x["rel_err"] for x in r["fd"]] or [0.0]),
+                "adjoint_stats": r["adjoint_stats"], "gmres_iters_forward": r["gmres_iters_forward"],
+                "gs_sweeps_forward": r["gs_sweeps_forward"]}
+        print(json.dumps(line), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     dtype = "f64" if wl.precision == 0 else "f32+f64"
     config = {"workload": wl.name, "grid_nx_ny_nz": [wl.nx, wl.ny_wall, wl.nz_span],
@@ -284,10 +352,14 @@ def main():
     tg = groups[top]
     launches_top = tg["launch_groups"]
     achieved = tg["bytes"] / (tg["ms"] * 1e-3) / 1e9 if tg["ms"] > 0 else 0.0
-    traffic = traffic_table().get(top)
+    tt = traffic_table().get(top)
+    traffic = tt.get("bytes_per_launch") if isinstance(tt, dict) else tt
     roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": traffic, "share_of_step": tg["ms"] / (r["elapsed"] * 1e3),
+                "traffic": traffic,
+                "traffic_note": (f"ncu dram bytes of one {tt['launch']} vs {tt['algorithmic_bytes_per_launch']:.0f} "
+                                 f"algorithmic ({tt['source']})") if isinstance(tt, dict) else None,
+                "share_of_step": tg["ms"] / (r["elapsed"] * 1e3),
                 "per_launch_ms": tg["ms"] / max(launches_top, 1)}
     step_bytes = sum(v["bytes"] for v in groups.values())
     line = {"metric": metric, "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": K,

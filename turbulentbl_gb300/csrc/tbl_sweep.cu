@@ -135,7 +135,7 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // row above by shuffle or, for lane 0, from global memory.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
-    constexpr int CH = 32 / sizeof(Val);  // points per lane per step: one 32-byte sector
+    constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
     const Geom& g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const SweepCta cta = a.ctas[blockIdx.x];
