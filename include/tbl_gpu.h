@@ -69,7 +69,7 @@ typedef struct tbl_config {
     int32_t mmax;           /* max GS sweeps and max GMRES restarts (reference: 1000, :139) */
     int32_t precision;      /* TBL_PREC_* */
     int32_t flags;          /* TBL_FLAG_* */
-    int32_t mixed_kmax;     /* inner FP32 GMRES restart length (mixed mode) */
+    int32_t mixed_kmax;     /* inner FP32 GMRES restart length (mixed mode), 1..63 */
     int32_t mixed_max_outer;/* max FP64 refinement sweeps (mixed mode) */
     double dt;              /* time step (reference: 1e-4, :34) */
     double re;              /* Reynolds number (reference: 150.92, :48) */
@@ -222,6 +222,68 @@ int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches
 #define TBL_NOALLOC_MAX_POINTS ((int64_t)TBL_NOALLOC_BLOCKS * 256 * 64)
 int tbl_div_diag_noalloc(const tbl_config* cfg, const double* jacinv, const double* u, const double* v,
                          const double* w, double* out);
+
+/* ---- Wall control and the discrete adjoint of a window of steps ---------
+ * The reference has no adjoint; it holds w = 0 at the wall
+ * (dnstbl2/dnstbl.f90:1317-1319).  tbl_set_wall_control replaces that value
+ * of w with a steady blowing/suction profile c, used by every later step:
+ *   w(i, j, k=1) = c[(i-1) + nx*(j-2)]   for i = 1..nx, j = 2..ny-1 (1-based)
+ * (nx*(ny-2) doubles; the spanwise ghost rows follow by the periodic copy).
+ * c = NULL restores w = 0.  FP64 and mixed handles alike. */
+int tbl_set_wall_control(tbl_handle* h, const double* c);
+
+/* Objective of a window of W steps: the time average over the steps of the
+ * span- and patch-averaged wall shear (dw/dx + du/dz)/Re at the wall,
+ * with the reference's wall-shear stencils (dnstbl2/dnstbl.f90:1636-1660:
+ * 6th-order central dw/dx, 2nd order within 3 points of the i ends;
+ * one-sided 2nd-order du/dz on the stretched grid) over the columns
+ * i = 2..nx-1 whose x1(i) lies in [x_lo, x_hi]. */
+typedef struct {
+    double x_lo, x_hi;    /* streamwise extent of the wall-shear patch */
+    int32_t ckpt_every;   /* checkpoint interval in steps (>= 1) */
+    int32_t pad_;
+} tbl_window_config;
+
+/* Host field pointers (the reference layout, nx*ny*nz doubles; NULL = none). */
+typedef struct {
+    double *u, *v, *w, *p;
+} tbl_fields;
+
+typedef struct {
+    int32_t steps;             /* W */
+    int32_t recomputed_steps;  /* forward steps re-run from checkpoints */
+    int32_t adj_gs_sweeps;     /* Gauss-Seidel sweeps of the transposed solves */
+    int32_t adj_gmres_iters;   /* GMRES iterations of the transposed Poisson solves */
+    int32_t status, pad_;
+    double max_gs_resid;       /* worst final relative residual of the transposed solves */
+    double max_gmres_resid;
+    double forward_ms;         /* host wall time of the last tbl_forward_window */
+    double backward_ms;        /* host wall time of this tbl_backward_window */
+} tbl_adjoint_stats;
+
+/* Advance nsteps steps exactly as tbl_step does (FP64 handles), recording a
+ * checkpoint of the state every wc->ckpt_every steps for a later
+ * tbl_backward_window, and return the window objective in *objective.  The
+ * recycling means, Wt, new(k) and lamda must stay fixed over the window: a
+ * window that would reach a rescaling step (every `cum` steps) is rejected
+ * with TBL_ERR_BAD_ARG, as is a replay handle. */
+int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* wc, double* objective,
+                       tbl_step_stats* stats);
+
+/* Discrete adjoint of the last forward window (reverse sweep over the
+ * recorded checkpoints, recomputing each segment's steps).  The map
+ * differentiated is the step with converged solves: the implicit-diffusion
+ * and pressure-Poisson adjoints are solves with the transposed operators
+ * (same Gauss-Seidel / SSOR-GMRES code, transposed wall-normal
+ * coefficients, the handle's errorstop / errtol), and the branch decisions
+ * (Peclet windows, upwind sides) are those of the recorded trajectory.
+ *   dL_dJ       weight of the window objective in the loss L
+ *   dL_dfinal   dL/d(state after the window) (u, v, w, p), or NULL
+ *   dL_dc       out: dL/dc, nx*(ny-2) doubles (layout of tbl_set_wall_control)
+ *   dL_dinitial out: dL/d(state before the window), or NULL
+ * Afterwards the handle holds the state at the end of the window again. */
+int tbl_backward_window(tbl_handle* h, double dL_dJ, const tbl_fields* dL_dfinal, double* dL_dc,
+                        tbl_fields* dL_dinitial, tbl_adjoint_stats* stats);
 
 /* Release everything. */
 void tbl_destroy(tbl_handle* h);

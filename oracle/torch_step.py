@@ -111,6 +111,7 @@ class TorchStep:
                     for cc, s2 in enumerate((rc["usum2"], rc["vsum2"], rc["wsum2"])):
                         U[cc] = U[cc].index_put((torch.tensor([0]), torch.arange(1, ny - 1), torch.tensor([k])),
                                                 torch.full((ny - 2,), float(s2[ir, k]), dtype=D))
+        self.last_u1 = [u.detach().clone() for u in U]  # velocities after the inflow
         # a2, a3 convection and Q (:621-768)
         Q = self._conv_q(U, P)
         # a4 implicit diffusion: exact solve of (1 - dt/Re L7) U* = Q

@@ -105,6 +105,26 @@ class TblStatsOut(C.Structure):
     ]
 
 
+class TblWindowConfig(C.Structure):
+    _fields_ = [("x_lo", C.c_double), ("x_hi", C.c_double), ("ckpt_every", C.c_int32), ("pad_", C.c_int32)]
+
+
+class TblFields(C.Structure):
+    _fields_ = [("u", _dp), ("v", _dp), ("w", _dp), ("p", _dp)]
+
+
+class TblAdjointStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32), ("recomputed_steps", C.c_int32), ("adj_gs_sweeps", C.c_int32),
+        ("adj_gmres_iters", C.c_int32), ("status", C.c_int32), ("pad_", C.c_int32),
+        ("max_gs_resid", C.c_double), ("max_gmres_resid", C.c_double),
+        ("forward_ms", C.c_double), ("backward_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad_"}
+
+
 STATS_FIELDS = ["usum", "vsum", "wsum", "uusum", "vvsum", "wwsum", "uvsum", "uwsum", "vwsum"]
 STATE_FIELDS_3D = ["u", "v", "w", "p", "pcorr", "uf", "vf", "wf"]
 STATE_FIELDS_2D = ["usum2", "vsum2", "wsum2", "wt"]

@@ -55,20 +55,20 @@ int prof_drain(tbl_handle* h) {
     return TBL_OK;
 }
 
-static int readback(tbl_handle* h, const void* dev, size_t bytes) {
+int readback(tbl_handle* h, const void* dev, size_t bytes) {
     TBL_CUDA_TRY(cudaMemcpyAsync(h->hpin, dev, bytes, cudaMemcpyDeviceToHost, h->stream));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return TBL_OK;
 }
 
 // 3-D host (nx,ny,nz) <-> device (sx,ny,nz)
-static int put3(tbl_handle* h, double* dst, const double* src) {
+int put3(tbl_handle* h, double* dst, const double* src) {
     const Geom& g = h->g;
     TBL_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)g.sx * 8, src, (size_t)g.nx * 8, (size_t)g.nx * 8,
                                    (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
     return TBL_OK;
 }
-static int get3(tbl_handle* h, double* dst, const double* src) {
+int get3(tbl_handle* h, double* dst, const double* src) {
     const Geom& g = h->g;
     TBL_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)g.nx * 8, src, (size_t)g.sx * 8, (size_t)g.nx * 8,
                                    (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, h->stream));
@@ -112,7 +112,7 @@ static int dalloc(T** p, size_t n) {
 
 static void free_all(tbl_handle* h) {
     void* mptrs[] = {h->Uf[0], h->Uf[1], h->Uf[2], h->Pf, h->Qf[0], h->Qf[1], h->Qf[2], h->Df[0], h->Df[1],
-                     h->Df[2], h->Vf, h->RHf, h->R64};
+                     h->Df[2], h->Vf, h->RHf, h->R64, h->lsg_partial, h->lsg_count, h->lsg_L, h->lsg_d, h->lsg_g};
     for (void* p : mptrs)
         if (p) cudaFree(p);
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
@@ -122,6 +122,10 @@ static void free_all(tbl_handle* h) {
                     h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    adj_free(h);
+    if (h->wallw) cudaFree(h->wallw);
+    if (h->AbT) cudaFree(h->AbT);
+    if (h->AtT) cudaFree(h->AtT);
     if (h->hpin) cudaFreeHost(h->hpin);
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -160,6 +164,12 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
         TRY(dalloc(&h->Pf, vol));
         TRY(dalloc(&h->RHf, vol));
         TRY(dalloc(&h->Vf, vol * (size_t)(cfg->mixed_kmax + 1)));
+        const int K1m = cfg->mixed_kmax + 1, ngr = (K1m + 7) / 8;
+        TRY(dalloc(&h->lsg_partial, (size_t)2 * 8 * ngr * 2048));
+        TRY(dalloc(&h->lsg_count, (size_t)ngr));
+        TRY(dalloc(&h->lsg_L, (size_t)K1m * K1m));
+        TRY(dalloc(&h->lsg_d, (size_t)K1m));
+        TRY(dalloc(&h->lsg_g, (size_t)K1m));
     } else {
         for (int c = 0; c < 3; ++c) { TRY(dalloc(&h->U[c], vol)); TRY(dalloc(&h->Q[c], vol)); }
         TRY(dalloc(&h->Pr, vol)); TRY(dalloc(&h->RH, vol));
@@ -207,6 +217,12 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TBL_CUDA_TRY(cudaMemcpy(h->At, At.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->Ap, Ap.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->rAp, rAp.data(), nz * 8, cudaMemcpyHostToDevice));
+    std::vector<double> AbT(nz, 0.0), AtT(nz, 0.0);  // L7^T: row k couples k-1 by At[k-1], k+1 by Ab[k+1]
+    for (int k = 1; k <= nz - 2; ++k) { AbT[k] = At[k - 1]; AtT[k] = Ab[k + 1]; }
+    TRY(dalloc(&h->AbT, (size_t)nz)); TRY(dalloc(&h->AtT, (size_t)nz));
+    TBL_CUDA_TRY(cudaMemcpy(h->AbT, AbT.data(), nz * 8, cudaMemcpyHostToDevice));
+    TBL_CUDA_TRY(cudaMemcpy(h->AtT, AtT.data(), nz * 8, cudaMemcpyHostToDevice));
+    h->x1h.assign(mesh->x1, mesh->x1 + nx);
     std::vector<int> sok(nz, 0);
     for (int r = 0; r < h->P; ++r)
         for (int k = h->bn[r]; k <= h->en[r]; ++k) sok[k] = r;
@@ -225,7 +241,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
 }
 
 // ------------------------------------------------------------ GS solve
-static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
+int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok) {
     const int mmax = h->cfg.mmax;
     bool active[3] = {true, true, true};
     int sweeps[3] = {0, 0, 0};
@@ -251,6 +267,11 @@ static int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st) {
             for (int q = 0; q < n; ++q) {
                 int c = comps[q];
                 double diver = red[c];
+                if (it == 1 && zero_ok && diver == 0.0) {  // zero right-hand side: the zero guess is exact
+                    active[c] = false;
+                    sumav[c] = 0.0;
+                    continue;
+                }
                 if (it == 1) sumnor[c] = 1.0 / diver;
                 sumav[c] = diver * sumnor[c];
                 bool stop = target ? (sweeps[c] >= target[c]) : (sumav[c] < h->cfg.errorstop);
@@ -331,12 +352,10 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
             }
             double* hcol = h->h + (size_t)K1 * (kit - 1);
             {
-                ProfScope ps(h, TBL_PROF_MGS, (2.0 + 4.0 * (kit - 1) + 3.0) * wN);
-                TRY(launch_mgs_f(h, W, nullptr, nullptr, V0, &hcol[0], 0));
-                for (int kk = 1; kk <= kit - 1; ++kk)
-                    TRY(launch_mgs_f(h, W, h->Vf + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->Vf + (size_t)kk * vol,
-                                     &hcol[kk], 0));
-                TRY(launch_mgs_f(h, W, h->Vf + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
+                // low-synch MGS: one dot pass over the basis (+1 vector per extra group), one update pass
+                const int ngr = (kit + 7) / 8;
+                ProfScope ps(h, TBL_PROF_MGS, ((kit + 2.0 * ngr) + (kit + 2.0)) * wN);
+                TRY(launch_lsg_f(h, W, kit, hcol));
             }
             {
                 ProfScope ps(h, TBL_PROF_SMALL, 0.0);
@@ -365,7 +384,7 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
 }
 
 // ------------------------------------------------------------ GMRES
-static int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_step_stats& st) {
+int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_step_stats& st) {
     const int kmax = h->cfg.kmax, K1 = kmax + 1;
     const size_t vol = (size_t)h->g.vol;
     double sumav = 1.0;
@@ -445,7 +464,7 @@ static int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, 
     return status;
 }
 
-static int one_step(tbl_handle* h, tbl_step_stats* out) {
+int one_step(tbl_handle* h, tbl_step_stats* out) {
     tbl_step_stats st;
     memset(&st, 0, sizeof(st));
     const tbl_config& c = h->cfg;
@@ -468,12 +487,16 @@ static int one_step(tbl_handle* h, tbl_step_stats* out) {
         ProfScope ps(h, TBL_PROF_BC, 0.0);
         TRY(launch_save_uold(h));
         if (h->nstep > c.recycle_after) TRY(launch_inflow(h));
+        if (h->tape_u1)  // adjoint window: the velocities the convection sees
+            for (int q = 0; q < 3; ++q)
+                TBL_CUDA_TRY(cudaMemcpyAsync(h->tape_u1 + (size_t)q * h->g.vol, h->U[q], (size_t)h->g.vol * 8,
+                                             cudaMemcpyDeviceToDevice, h->stream));
     }
     {
         ProfScope ps(h, TBL_PROF_CONV, 7.0 * wN);
         TRY(launch_conv_q(h));
     }
-    TRY(gs_solve(h, replay ? gs_target : nullptr, st));
+    TRY(gs_solve(h, replay ? gs_target : nullptr, st, false));
     {
         ProfScope ps(h, TBL_PROF_BC, 4.0 * wN);
         TRY(launch_div(h));
@@ -558,7 +581,7 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
     if (cfg->kmax < 1 || cfg->mmax < 1 || !(cfg->dt > 0) || !(cfg->re > 0)) return TBL_ERR_BAD_ARG;
     if (cfg->precision != TBL_PREC_FP64 && cfg->precision != TBL_PREC_MIXED) return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED &&
-        (cfg->mixed_kmax < 1 || cfg->mixed_max_outer < 1 || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
+        (cfg->mixed_kmax < 1 || cfg->mixed_kmax > 63 || cfg->mixed_max_outer < 1 || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
         return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED && (cfg->flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
     int ndev = 0;

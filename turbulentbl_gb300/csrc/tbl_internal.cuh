@@ -70,6 +70,8 @@ struct RedWork {
     int max_blocks;
 };
 
+struct AdjTape;  // tbl_adjoint.cu
+
 template <typename T>
 struct Fields {
     T* U[3];
@@ -103,6 +105,9 @@ struct tbl_handle {
     float* Vf;       // inner Krylov vectors
     float* RHf;      // inner SSOR work
     double* R64;     // FP64 outer residual
+    double* lsg_partial;        // low-synch Gram-Schmidt: per-block partials [2*8*groups][max_blocks]
+    unsigned int* lsg_count;    // arrival counters per group
+    double *lsg_L, *lsg_d, *lsg_g;  // (K1 x K1) strictly lower Gram matrix, Q^T w, Q^T v_new
     // per-k coefficient arrays and mesh (nz)
     double *x3, *jacinv, *jac2, *Ab, *At, *Ap, *rAp;
     // recycling state
@@ -145,6 +150,12 @@ struct tbl_handle {
     size_t replay_pos;
     std::vector<int32_t> last_counts;
     double lamda_host;
+    // wall control and the adjoint window (tbl_adjoint.cu)
+    double* wallw;          // nx*(ny-2) wall-normal wall velocity, null = 0
+    double *AbT, *AtT;      // transposed wall-normal coefficients: AbT[k] = At[k-1], AtT[k] = Ab[k+1]
+    double* tape_u1;        // when set, one_step copies the post-inflow velocities here (3 x vol)
+    tbl::AdjTape* adj;
+    std::vector<double> x1h;  // host copy of x1
     // kernel-group timing (tbl_profile)
     struct ProfMark { int group; int e0, e1; double bytes; };
     bool prof_on;

@@ -44,5 +44,17 @@ int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom);
 int launch_backsub_update_f(tbl_handle* h, int kit);
 int launch_restart_init_k(tbl_handle* h, int first, int K1);
 int launch_givens_k(tbl_handle* h, int kit, int K1);
+int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol);
+
+// tbl_api.cu
+int readback(tbl_handle* h, const void* dev, size_t bytes);
+int put3(tbl_handle* h, double* dst, const double* src);
+int get3(tbl_handle* h, double* dst, const double* src);
+int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok);
+int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_step_stats& st);
+int one_step(tbl_handle* h, tbl_step_stats* out);
+
+// tbl_adjoint.cu
+void adj_free(tbl_handle* h);
 
 }  // namespace tbl

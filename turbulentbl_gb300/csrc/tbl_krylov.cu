@@ -232,16 +232,18 @@ __global__ void k_scale_inv_f(long long n4, float4* __restrict__ w, const double
     }
 }
 
-// p' (FP64) += sum_i y_i v_i (FP32 vectors), accumulated in FP64
+// p' (FP64) += sum_i y_i v_i: the FP32 correction of one inner cycle, added in FP64
 __global__ void k_update_f(long long n4, double* __restrict__ pc, const float4* __restrict__ V, long long vstride4,
                            const double* __restrict__ gy, int kit) {
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
-        double4 x = reinterpret_cast<double4*>(pc)[q];
+        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int i = 0; i < kit; ++i) {
-            float4 v = V[(long long)i * vstride4 + q];
-            double y = gy[i];
-            x.x += (double)v.x * y; x.y += (double)v.y * y; x.z += (double)v.z * y; x.w += (double)v.w * y;
+            const float4 v = V[(long long)i * vstride4 + q];
+            const float y = (float)gy[i];
+            c.x = fmaf(y, v.x, c.x); c.y = fmaf(y, v.y, c.y); c.z = fmaf(y, v.z, c.z); c.w = fmaf(y, v.w, c.w);
         }
+        double4 x = reinterpret_cast<double4*>(pc)[q];
+        x.x += (double)c.x; x.y += (double)c.y; x.z += (double)c.z; x.w += (double)c.w;
         reinterpret_cast<double4*>(pc)[q] = x;
     }
 }
@@ -290,6 +292,149 @@ int launch_backsub_update(tbl_handle* h, int kit) {
     k_update<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)h->PC, (const double2*)h->V, h->g.vol / 2,
                                                 h->gy, kit);
     h->launches += 2;
+    return TBL_OK;
+}
+
+// ------------------------- low-synchronisation Gram-Schmidt (FP32 inner GMRES)
+// Modified Gram-Schmidt in its inverse compact-WY form: for a basis
+// Q = [v_0 .. v_{n-1}] with L the strictly lower triangle of Q^T Q, the product
+// of the n MGS projections is I - Q (I + L)^-1 Q^T (exactly, also when Q has
+// lost orthogonality).  One pass forms Q^T w and the new row of L
+// (Q^T v_{n-1}); a forward substitution gives the Hessenberg column t; a
+// second pass applies w -= Q t and forms ||w||.  2n+3 vector passes per
+// Arnoldi step instead of MGS's 4n+1; the FP64 outer refinement of the mixed
+// solve makes the different rounding irrelevant to the final accuracy.
+constexpr int LSG_G = 8;  // basis vectors per group (grid.y) of the dot pass
+
+__device__ __forceinline__ float dot4f(float4 a, float4 b) {
+    return fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
+}
+
+// d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the group's i; per-thread FP32
+// partials over up to 4 float4 (16 products) are accumulated in FP64, blocks
+// reduce in FP64 and the last block of each group sums the partials in block
+// order (deterministic).
+__global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
+                                                            const float4* __restrict__ V, long long vstride4, int nv,
+                                                            double* __restrict__ partial, unsigned int* __restrict__ count,
+                                                            int max_blocks, double* __restrict__ dout,
+                                                            double* __restrict__ gout) {
+    __shared__ double s_red[RED_THREADS / 32];
+    __shared__ bool s_last;
+    const int i0 = blockIdx.y * LSG_G;
+    const int ng = min(LSG_G, nv - i0);
+    const float4* vl = V + (long long)(nv - 1) * vstride4;
+    double ad[LSG_G], ag[LSG_G];
+#pragma unroll
+    for (int e = 0; e < LSG_G; ++e) { ad[e] = 0.0; ag[e] = 0.0; }
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < n4; q0 += 4 * stride) {
+        float fd[LSG_G], fg[LSG_G];
+#pragma unroll
+        for (int e = 0; e < LSG_G; ++e) { fd[e] = 0.f; fg[e] = 0.f; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long q = q0 + u * stride;
+            if (q < n4) {
+                const float4 x = w[q], l = vl[q];
+#pragma unroll
+                for (int e = 0; e < LSG_G; ++e)
+                    if (e < ng) {
+                        const float4 v = V[(long long)(i0 + e) * vstride4 + q];
+                        fd[e] += dot4f(v, x);
+                        fg[e] += dot4f(v, l);
+                    }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < LSG_G; ++e) { ad[e] += (double)fd[e]; ag[e] += (double)fg[e]; }
+    }
+    const size_t base = (size_t)blockIdx.y * 2 * LSG_G;
+#pragma unroll
+    for (int e = 0; e < LSG_G; ++e) {
+        if (e >= ng) break;
+        const double bd = block_sum(ad[e], s_red);
+        const double bg = block_sum(ag[e], s_red);
+        if (threadIdx.x == 0) {
+            partial[(base + 2 * e) * max_blocks + blockIdx.x] = bd;
+            partial[(base + 2 * e + 1) * max_blocks + blockIdx.x] = bg;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&count[blockIdx.y], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int v = 0; v < 2 * ng; ++v) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&partial[(base + v) * max_blocks + b]);
+        acc = block_sum(acc, s_red);
+        if (threadIdx.x == 0) {
+            const int i = i0 + v / 2;
+            if (v % 2 == 0) dout[i] = acc;
+            else if (i < nv - 1) gout[i] = acc;
+        }
+    }
+    if (threadIdx.x == 0) count[blockIdx.y] = 0u;
+}
+
+// New row of L (row nv-1: <v_{nv-1}, v_j>, j < nv-1), then (I + L) t = d by
+// forward substitution into the Hessenberg column.  Rows of older vectors
+// were written when each was the newest.
+__global__ void k_lsg_solve(int K1, int nv, double* __restrict__ Lm, const double* __restrict__ d,
+                            const double* __restrict__ gnew, double* __restrict__ hcol) {
+    if (threadIdx.x != 0) return;
+    const int r = nv - 1;
+    for (int j = 0; j < r; ++j) Lm[(size_t)r * K1 + j] = gnew[j];
+    for (int i = 0; i < nv; ++i) {
+        double t = d[i];
+        for (int j = 0; j < i; ++j) t -= Lm[(size_t)i * K1 + j] * hcol[j];
+        hcol[i] = t;
+    }
+}
+
+// w -= sum_i t_i v_i (FP32), then ||w|| -> *out (sqrt of the deterministic sum)
+__global__ void __launch_bounds__(RED_THREADS) k_lsg_update_f(long long n4, float4* __restrict__ w,
+                                                              const float4* __restrict__ V, long long vstride4, int nv,
+                                                              const double* __restrict__ t, RedWork rw, int slot,
+                                                              double* out) {
+    __shared__ double s_red[RED_THREADS / 32];
+    __shared__ float s_t[64];
+    for (int i = threadIdx.x; i < nv && i < 64; i += blockDim.x) s_t[i] = (float)t[i];
+    __syncthreads();
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+        float4 x = w[q];
+        for (int i = 0; i < nv; ++i) {
+            const float4 v = V[(long long)i * vstride4 + q];
+            const float ti = s_t[i];
+            x.x = fmaf(-ti, v.x, x.x);
+            x.y = fmaf(-ti, v.y, x.y);
+            x.z = fmaf(-ti, v.z, x.z);
+            x.w = fmaf(-ti, v.w, x.w);
+        }
+        w[q] = x;
+        acc += (double)dot4f(x, x);
+    }
+    const double bt = block_sum(acc, s_red);
+    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, 1);
+}
+
+int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
+    const int K1 = h->cfg.mixed_kmax + 1;
+    if (kit > 64 || kit > K1) return TBL_ERR_BAD_ARG;
+    const int nb = red_blocks(h);
+    const long long n4 = h->g.vol / 4;
+    dim3 grid(nb, (kit + LSG_G - 1) / LSG_G);
+    k_lsg_dots_f<<<grid, RED_THREADS, 0, h->stream>>>(n4, (const float4*)W, (const float4*)h->Vf, n4, kit,
+                                                      h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d,
+                                                      h->lsg_g);
+    k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);
+    k_lsg_update_f<<<nb, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
+                                                      &hcol[kit]);
+    h->launches += 3;
     return TBL_OK;
 }
 

@@ -312,17 +312,21 @@ __global__ void __launch_bounds__(128) k_project(Geom g, double invdx, double in
     U3[p] = (T)((double)U3[p] - (dt * g3));
 }
 
-// velocity BCs, wall and top (:1317-1330), one thread per (i, j unique)
+// velocity BCs, wall and top (:1317-1330), one thread per (i, j unique).
+// wallw (nx*(ny-2), or null for the reference's w = 0) is the wall-normal
+// blowing/suction velocity set by tbl_set_wall_control.
 template <typename T>
-__global__ void k_vel_bc_walltop(Geom g, T* __restrict__ U1, T* __restrict__ U2, T* __restrict__ U3) {
+__global__ void k_vel_bc_walltop(Geom g, T* __restrict__ U1, T* __restrict__ U2, T* __restrict__ U3,
+                                 const double* __restrict__ wallw) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int J = g.ny - 2;
     if (t >= g.nx * J) return;
     int i = t % g.nx, j = 1 + t / g.nx;
     int nz = g.nz;
     T* Us[3] = {U1, U2, U3};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) Us[c][idx(g, i, j, 0)] = T(0);
+    Us[0][idx(g, i, j, 0)] = T(0);
+    Us[1][idx(g, i, j, 0)] = T(0);
+    Us[2][idx(g, i, j, 0)] = wallw ? (T)wallw[t] : T(0);
 #pragma unroll
     for (int c = 0; c < 3; ++c)
         Us[c][idx(g, i, j, nz - 1)] =
@@ -797,7 +801,7 @@ static void project_bcs_t(tbl_handle* h, T* U0, T* U1, T* U2, T* Pr) {
     k_pc_bc_inout<<<(n3 + 255) / 256, 256, 0, h->stream>>>(g, h->PC);
     k_project<T><<<interior_grid(g), 128, 0, h->stream>>>(g, 1.0 / c.dx, 1.0 / c.dy, 1.0 / c.dxi, c.dt, h->jacinv,
                                                           h->PC, Pr, U0, U1, U2);
-    k_vel_bc_walltop<T><<<(n1 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2);
+    k_vel_bc_walltop<T><<<(n1 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2, h->wallw);
     k_vel_bc_out<T><<<(n3 + 255) / 256, 256, 0, h->stream>>>(g, U0, U1, U2);
     PbcCoef pc;
     pc.dx = c.dx; pc.dy = c.dy; pc.dxi = c.dxi; pc.re = c.re; pc.dt = c.dt;
