@@ -151,6 +151,11 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
         if (r == h->P - 1) h->en[r] = nz - 2;
     }
     TBL_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    {
+        int dev = 0;
+        TBL_CUDA_TRY(cudaGetDevice(&dev));
+        TBL_CUDA_TRY(cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, dev));
+    }
     TBL_CUDA_TRY(cudaMallocHost(&h->hpin, 4096));
     const size_t vol = (size_t)g.vol, n2 = (size_t)nx * nz, pl = (size_t)ny * nz;
     TRY(dalloc(&h->PC, vol));

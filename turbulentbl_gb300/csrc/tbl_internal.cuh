@@ -145,6 +145,7 @@ struct tbl_handle {
     double time;
     bool fluc_updated;
     int coop_ok;
+    int n_sm;                      // multiprocessors of the device
     // replay
     std::vector<int32_t> replay;
     size_t replay_pos;

@@ -12,16 +12,20 @@
 
 namespace tbl {
 
+// Grid of the streaming reductions: one resident wave (8 blocks of 256 threads
+// per SM), so no partial second wave idles part of the GPU at the tail.
 int red_blocks(tbl_handle* h) {
     long long n2 = h->g.vol / 2;
     long long b = (n2 + RED_THREADS * 4 - 1) / (RED_THREADS * 4);
+    const long long wave = 8LL * (h->n_sm > 0 ? h->n_sm : 148);
+    if (b > wave) b = wave;
     if (b > h->red.max_blocks) b = h->red.max_blocks;
     if (b < 1) b = 1;
     return (int)b;
 }
 
 // sum(a*b) over the volume -> *out (op 1: sqrt)
-__global__ void __launch_bounds__(RED_THREADS) k_dot(long long n2, const double2* __restrict__ a,
+__global__ void __launch_bounds__(RED_THREADS, 8) k_dot(long long n2, const double2* __restrict__ a,
                                                      const double2* __restrict__ b, RedWork rw, int slot,
                                                      double* out, int op) {
     __shared__ double s_red[RED_THREADS / 32];
@@ -38,7 +42,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot(long long n2, const double2
 // One modified Gram-Schmidt pass (:1140-1150):
 //   w -= (*hk) * vk          (skipped when vk == nullptr)
 //   *out = sum(vn * w)       (vn == nullptr: sum(w*w), op 1 takes the sqrt)
-__global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __restrict__ w,
+__global__ void __launch_bounds__(RED_THREADS, 8) k_mgs(long long n2, double2* __restrict__ w,
                                                      const double2* __restrict__ vk, const double* __restrict__ hk,
                                                      const double2* __restrict__ vn, RedWork rw, int slot,
                                                      double* out, int op) {
@@ -187,7 +191,7 @@ __device__ __forceinline__ double dot4(float4 a, float4 b) {
     return (double)fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_dot_f(long long n4, const float4* __restrict__ a,
+__global__ void __launch_bounds__(RED_THREADS, 8) k_dot_f(long long n4, const float4* __restrict__ a,
                                                        const float4* __restrict__ b, RedWork rw, int slot,
                                                        double* out, int op) {
     __shared__ double s_red[RED_THREADS / 32];
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot_f(long long n4, const float
     grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_mgs_f(long long n4, float4* __restrict__ w,
+__global__ void __launch_bounds__(RED_THREADS, 8) k_mgs_f(long long n4, float4* __restrict__ w,
                                                        const float4* __restrict__ vk, const double* __restrict__ hk,
                                                        const float4* __restrict__ vn, RedWork rw, int slot,
                                                        double* out, int op) {
@@ -396,7 +400,7 @@ __global__ void k_lsg_solve(int K1, int nv, double* __restrict__ Lm, const doubl
 }
 
 // w -= sum_i t_i v_i (FP32), then ||w|| -> *out (sqrt of the deterministic sum)
-__global__ void __launch_bounds__(RED_THREADS) k_lsg_update_f(long long n4, float4* __restrict__ w,
+__global__ void __launch_bounds__(RED_THREADS, 8) k_lsg_update_f(long long n4, float4* __restrict__ w,
                                                               const float4* __restrict__ V, long long vstride4, int nv,
                                                               const double* __restrict__ t, RedWork rw, int slot,
                                                               double* out) {
