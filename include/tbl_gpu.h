@@ -241,8 +241,18 @@ int tbl_set_wall_control(tbl_handle* h, const double* c);
 typedef struct {
     double x_lo, x_hi;    /* streamwise extent of the wall-shear patch */
     int32_t ckpt_every;   /* checkpoint interval in steps (>= 1) */
-    int32_t pad_;
+    int32_t branch_mode;  /* TBL_BRANCH_*: the convection's data-dependent decisions */
 } tbl_window_config;
+
+/* The convection switches stencils on Peclet windows and on the sign of the
+ * advecting velocity (:651-713), so the step is only piecewise smooth.  For
+ * checking gradients by finite differences a window can record those
+ * decisions (one byte per point and step) and later windows of the same
+ * length can replay them, which makes the forward map exactly the one the
+ * adjoint differentiates.  TBL_BRANCH_FREE is the reference behaviour. */
+#define TBL_BRANCH_FREE    0
+#define TBL_BRANCH_RECORD  1
+#define TBL_BRANCH_REPLAY  2
 
 /* Host field pointers (the reference layout, nx*ny*nz doubles; NULL = none). */
 typedef struct {

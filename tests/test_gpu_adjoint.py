@@ -178,6 +178,41 @@ def test_directional_derivatives_fd_and_tangent_linear(case):
     assert worst_tl <= TOL_TORCH, worst_tl
 
 
+def test_frozen_branch_record_is_the_free_run_and_replay_fd_is_exact(case):
+    """TBL_BRANCH_RECORD reproduces the free run; finite differences through
+    TBL_BRANCH_REPLAY (the recorded Peclet/sign decisions) follow exactly the
+    map the adjoint differentiates."""
+    from turbulentbl_gb300 import abi
+    g, x0, c = case["g"], case["x0"], case["c"]
+    J0 = _gpu_J(g, x0, c)
+    s0 = g.download()
+    g.upload(x0)
+    g.set_wall_control(c)
+    J1, _ = g.forward_window(W, PATCH[0], PATCH[1], 2, abi.TBL_BRANCH_RECORD)
+    s1 = g.download()
+    assert abs(J1 - J0) <= 1e-14 * abs(J0)
+    for f in ("u", "v", "w", "p"):
+        assert np.abs(s1[f] - s0[f]).max() <= 1e-13 * np.abs(s0[f]).max(), f
+    gc, _, _ = g.backward_window(1.0)
+    assert _rel(gc, case["gt"]) <= TOL_TORCH
+    rng = np.random.default_rng(77)
+    for _ in range(4):
+        d = rng.normal(0.0, 1e-3, c.shape)
+        eps = 1e-2
+        Jp = Jm = None
+        for sgn in (1, -1):
+            g.upload(x0)
+            g.set_wall_control(c + sgn * eps * d)
+            J, _ = g.forward_window(W, PATCH[0], PATCH[1], 2, abi.TBL_BRANCH_REPLAY)
+            if sgn > 0:
+                Jp = J
+            else:
+                Jm = J
+        fd = (Jp - Jm) / (2 * eps)
+        ad = float((gc * d).sum())
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
 class _WindowObjective(torch.autograd.Function):
     """torch.autograd wrapper over the C ABI: J(c) forward, dJ/dc backward."""
 

@@ -40,6 +40,10 @@ TBL_FLAG_REPLAY = 1
 TBL_FLAG_PPE_RESIDUAL = 2
 TBL_FLAG_DIAGNOSTICS = 4
 
+TBL_BRANCH_FREE = 0
+TBL_BRANCH_RECORD = 1
+TBL_BRANCH_REPLAY = 2
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 
@@ -106,7 +110,7 @@ class TblStatsOut(C.Structure):
 
 
 class TblWindowConfig(C.Structure):
-    _fields_ = [("x_lo", C.c_double), ("x_hi", C.c_double), ("ckpt_every", C.c_int32), ("pad_", C.c_int32)]
+    _fields_ = [("x_lo", C.c_double), ("x_hi", C.c_double), ("ckpt_every", C.c_int32), ("branch_mode", C.c_int32)]
 
 
 class TblFields(C.Structure):

@@ -62,6 +62,9 @@ struct AdjTape {
     double *lc = nullptr, *AW = nullptr, *LE = nullptr, *luold = nullptr;
     double *ocf = nullptr, *jacc = nullptr;
     std::vector<int> nstep_of;
+    unsigned char* bits = nullptr;  // W x vol frozen-branch record (TBL_BRANCH_RECORD / _REPLAY)
+    int branch_mode = TBL_BRANCH_FREE;
+    bool bits_valid = false;        // a record of this window length exists
     bool valid = false;
     double forward_ms = 0.0;
 };
@@ -432,13 +435,16 @@ struct ConvAdjCoef {
 // Stencil coefficients cf[o+2] (o = -2..2) of the convection term along one
 // direction at a point with multiplier m (u, v or w there); dir 1 is the
 // spanwise direction with its first-order upwind rows.
+// b >= 0: frozen-branch record byte (bit 3+dir' sign of |m|; bits 4/5 the
+// spanwise upwind sides), else the signs of m itself.
 __device__ __forceinline__ void conv_stencil(int dir, double m, bool nearb, bool win, double inv2, double q25,
-                                             double c12, double invdy, double cf[5]) {
+                                             double c12, double invdy, double cf[5], int b = -1) {
 #pragma unroll
     for (int o = 0; o < 5; ++o) cf[o] = 0.0;
     if (nearb) {
         if (dir == 1) {
-            const double ap = fmax(m, 0.0), bn = fmin(m, 0.0);
+            const double ap = b >= 0 ? ((b & 16) ? m : 0.0) : fmax(m, 0.0);
+            const double bn = b >= 0 ? ((b & 32) ? m : 0.0) : fmin(m, 0.0);
             cf[2] = (ap - bn) * invdy;
             cf[1] = -ap * invdy;
             cf[3] = bn * invdy;
@@ -448,7 +454,8 @@ __device__ __forceinline__ void conv_stencil(int dir, double m, bool nearb, bool
         }
         return;
     }
-    const double a = fabs(m);
+    const int sbit = dir == 0 ? 8 : (dir == 1 ? 16 : 64);
+    const double a = b >= 0 ? ((b & sbit) ? m : -m) : fabs(m);
     if (win) {
         cf[4] = a * q25 - m * c12;
         cf[3] = -4.0 * a * q25 + 8.0 * m * c12;
@@ -464,9 +471,17 @@ __device__ __forceinline__ void conv_stencil(int dir, double m, bool nearb, bool
 }
 
 // Branch decision of the forward convection at interior point (i,j,k) along dir
-// (sign(1, ceiling(m)) Peclet test as in the forward kernels).
+// (sign(1, ceiling(m)) Peclet test as in the forward kernels), or from the
+// frozen-branch record byte b (b >= 0; bits 0-2 the x/y/z windows).
 __device__ __forceinline__ void conv_case(const Geom& g, const ConvAdjCoef& c, const double* __restrict__ x3,
-                                          int dir, int i, int j, int k, double m, bool& nearb, bool& win) {
+                                          int dir, int i, int j, int k, double m, bool& nearb, bool& win,
+                                          int b = -1) {
+    if (b >= 0) {
+        nearb = dir == 0 ? ((i <= 1) || (i >= g.nx - 2)) : (dir == 1 ? ((j == 1) || (j == g.ny - 2))
+                                                                      : ((k <= 1) || (k >= g.nz - 2)));
+        win = (b >> dir) & 1;
+        return;
+    }
     const double sgn = m > -1.0 ? 1.0 : -1.0;
     if (dir == 0) {
         nearb = (i <= 1) || (i >= g.nx - 2);
@@ -495,7 +510,8 @@ __global__ void __launch_bounds__(128) k_adj_conv(Geom g, ConvAdjCoef c, double 
                                                   const double* __restrict__ w1, const double* __restrict__ nu0,
                                                   const double* __restrict__ nu1, const double* __restrict__ nu2,
                                                   double* __restrict__ l0, double* __restrict__ l1,
-                                                  double* __restrict__ l2, double* __restrict__ lP) {
+                                                  double* __restrict__ l2, double* __restrict__ lP,
+                                                  const unsigned char* __restrict__ bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y, k = blockIdx.z;
     const int nx = g.nx, nz = g.nz;
@@ -537,10 +553,11 @@ __global__ void __launch_bounds__(128) k_adj_conv(Geom g, ConvAdjCoef c, double 
             if (!inner(g, pi, pj, pk)) continue;
             const long long p = ix(g, pi, pj, pk);
             const double m = Us[d][p];
+            const int bp = bits ? (int)bits[p] : -1;
             bool nearb, win;
-            conv_case(g, c, x3, d, pi, pj, pk, m, nearb, win);
+            conv_case(g, c, x3, d, pi, pj, pk, m, nearb, win, bp);
             double cf[5];
-            conv_stencil(d, m, nearb, win, inv2, q25, c12, c.invdy, cf);
+            conv_stencil(d, m, nearb, win, inv2, q25, c12, c.invdy, cf, bp);
             double w = cf[o + 2];
             if (d == 2) w *= jacinv[pk];
             if (w != 0.0) {
@@ -552,14 +569,18 @@ __global__ void __launch_bounds__(128) k_adj_conv(Geom g, ConvAdjCoef c, double 
     // multiplier part at q itself: d conv / d(u, v, w)(q)
     if (qin) {
         const int ja = ring(g, j, -1), jb = ring(g, j, -2), jc = ring(g, j, 1), jd = ring(g, j, 2);
+        const int bq = bits ? (int)bits[q] : -1;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const double m = Us[d][q];
             bool nearb, win;
-            conv_case(g, c, x3, d, i, j, k, m, nearb, win);
+            conv_case(g, c, x3, d, i, j, k, m, nearb, win, bq);
             const double q25 = d == 0 ? c.q25x : (d == 1 ? c.q25y : c.q25z);
             const double c12 = d == 0 ? c.c12x : (d == 1 ? c.c12y : c.c12z);
-            const double sg = (m > 0.0) ? 1.0 : ((m < 0.0) ? -1.0 : 0.0);
+            const int sbit = d == 0 ? 8 : (d == 1 ? 16 : 64);
+            const double sg = bq >= 0 ? ((bq & sbit) ? 1.0 : -1.0) : ((m > 0.0) ? 1.0 : ((m < 0.0) ? -1.0 : 0.0));
+            const bool vpos = bq >= 0 ? (bq & 16) != 0 : m >= 0.0;
+            const bool vneg = bq >= 0 ? (bq & 32) != 0 : m <= 0.0;
             double acc = 0.0;
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) {
@@ -581,7 +602,7 @@ __global__ void __launch_bounds__(128) k_adj_conv(Geom g, ConvAdjCoef c, double 
                 double dm;
                 if (nearb) {
                     if (d == 1)
-                        dm = (m >= 0.0 ? (f[2] - f[1]) * c.invdy : 0.0) + (m <= 0.0 ? (f[3] - f[2]) * c.invdy : 0.0);
+                        dm = (vpos ? (f[2] - f[1]) * c.invdy : 0.0) + (vneg ? (f[3] - f[2]) * c.invdy : 0.0);
                     else
                         dm = (f[3] - f[1]) * (d == 0 ? c.inv2x : c.inv2z);
                 } else if (win) {
@@ -708,7 +729,8 @@ struct AdjCounters {
 // Adjoint of one step.  u1: velocities after the step's inflow (3 x vol),
 // u3: the step's output velocities.  T->lU / T->lP hold dL/d(output) on
 // entry and dL/d(input) on return; dL/dc accumulates in T->lc.
-int adj_step(tbl_handle* h, AdjTape* T, const double* u1, const double* u3, int nstep_of_step, AdjCounters& cnt) {
+int adj_step(tbl_handle* h, AdjTape* T, const double* u1, const double* u3, int nstep_of_step,
+             const unsigned char* bits, AdjCounters& cnt) {
     const Geom& g = h->g;
     const size_t vol = (size_t)g.vol;
     const AdjCoef ac = adj_coef(h);
@@ -764,7 +786,7 @@ int adj_step(tbl_handle* h, AdjTape* T, const double* u1, const double* u3, int 
     }
     k_adj_conv<<<full_grid(g), 128, 0, h->stream>>>(g, conv_adj_coef(h), ac.t, ac.aw, h->Ab, h->At, h->x3, h->jacinv,
                                                     u1, u1 + vol, u1 + 2 * vol, h->U[0], h->U[1], h->U[2], l0, l1,
-                                                    l2, lP);
+                                                    l2, lP, bits);
     const int inflow_on = nstep_of_step > h->cfg.recycle_after ? 1 : 0;
     k_adj_inflow<<<nblk(ny - 2, 128), 128, 0, h->stream>>>(g, inflow_on, h->cfg.irec - 1, h->cfg.ue, h->usum2, h->wt,
                                                           h->newk, h->slab_of_k, h->slabs, h->sc, T->luold, l0, l1,
@@ -875,6 +897,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 void adj_free(tbl_handle* h) {
     if (!h->adj) return;
     if (h->adj->buf) cudaFree(h->adj->buf);
+    if (h->adj->bits) cudaFree(h->adj->bits);
     delete h->adj;
     h->adj = nullptr;
 }
@@ -902,6 +925,7 @@ int tbl_set_wall_control(tbl_handle* h, const double* c) {
 int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* wc, double* objective,
                        tbl_step_stats* stats) {
     if (!h || !wc || nsteps < 1 || wc->ckpt_every < 1) return TBL_ERR_BAD_ARG;
+    if (wc->branch_mode < TBL_BRANCH_FREE || wc->branch_mode > TBL_BRANCH_REPLAY) return TBL_ERR_BAD_ARG;
     const tbl_config& c = h->cfg;
     if (c.precision != TBL_PREC_FP64 || (c.flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
     for (int s = 1; s <= nsteps; ++s)
@@ -914,6 +938,14 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
     T->valid = false;
     const Geom& g = h->g;
     const size_t vol = (size_t)g.vol;
+    const int bm = wc->branch_mode;
+    if (bm == TBL_BRANCH_REPLAY && !T->bits_valid) return TBL_ERR_BAD_ARG;  // no record of this window
+    if (bm != TBL_BRANCH_FREE && !T->bits) {
+        TBL_CUDA_TRY(cudaMalloc((void**)&T->bits, (size_t)nsteps * vol));
+        TBL_CUDA_TRY(cudaMemset(T->bits, 0, (size_t)nsteps * vol));
+    }
+    if (bm == TBL_BRANCH_RECORD) T->bits_valid = false;
+    T->branch_mode = bm;
     TBL_CUDA_TRY(cudaMemcpyAsync(T->ocf, cf.data(), cf.size() * 8, cudaMemcpyHostToDevice, h->stream));
     ATRY(dzero(h, T->jacc, 1));
     const auto t0 = std::chrono::steady_clock::now();
@@ -922,8 +954,12 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
         if (s % ck == 0) ATRY(save_ckpt(h, T->cks[s / ck]));
         const bool rec = s >= last0;
         h->tape_u1 = rec ? T->segU1[s - last0] : nullptr;
+        h->conv_bits_mode = bm;
+        h->conv_bits = bm != TBL_BRANCH_FREE ? T->bits + (size_t)s * vol : nullptr;
         const int st = one_step(h, stats ? &stats[s] : nullptr);
         h->tape_u1 = nullptr;
+        h->conv_bits_mode = TBL_BRANCH_FREE;
+        h->conv_bits = nullptr;
         if (st != TBL_OK) return st;
         T->nstep_of[s] = h->nstep;
         if (rec)
@@ -938,6 +974,7 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
     ATRY(dcopy(h, T->fin_sums, h->sums, 9 * (size_t)g.nx * g.nz));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     T->forward_ms = ms_since(t0);
+    if (bm == TBL_BRANCH_RECORD) T->bits_valid = true;
     T->valid = true;
     if (objective) *objective = J;
     return TBL_OK;
@@ -969,8 +1006,14 @@ int tbl_backward_window(tbl_handle* h, double dL_dJ, const tbl_fields* dL_dfinal
             ATRY(restore_ckpt(h, T->cks[seg]));
             for (int s = s0; s < s1; ++s) {
                 h->tape_u1 = T->segU1[s - s0];
+                if (T->branch_mode != TBL_BRANCH_FREE) {  // the recorded decisions reproduce the window exactly
+                    h->conv_bits_mode = TBL_BRANCH_REPLAY;
+                    h->conv_bits = T->bits + (size_t)s * vol;
+                }
                 status = one_step(h, nullptr);
                 h->tape_u1 = nullptr;
+                h->conv_bits_mode = TBL_BRANCH_FREE;
+                h->conv_bits = nullptr;
                 if (status != TBL_OK) break;
                 for (int q = 0; q < 3; ++q) ATRY(dcopy(h, T->segU3[s - s0] + q * vol, h->U[q], vol));
                 recomputed++;
@@ -981,7 +1024,8 @@ int tbl_backward_window(tbl_handle* h, double dL_dJ, const tbl_fields* dL_dfinal
             k_objective_adj<<<nblk((long long)g.nx * (g.ny - 2), 256), 256, 0, h->stream>>>(
                 g, T->ocf, dL_dJ / W, T->lU[0], T->lU[2]);
             h->launches++;
-            status = adj_step(h, T, T->segU1[s - s0], T->segU3[s - s0], T->nstep_of[s], cnt);
+            status = adj_step(h, T, T->segU1[s - s0], T->segU3[s - s0], T->nstep_of[s],
+                              T->branch_mode != TBL_BRANCH_FREE ? T->bits + (size_t)s * vol : nullptr, cnt);
             if (status != TBL_OK) break;
         }
     }

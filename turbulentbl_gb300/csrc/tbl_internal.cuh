@@ -155,6 +155,8 @@ struct tbl_handle {
     double* wallw;          // nx*(ny-2) wall-normal wall velocity, null = 0
     double *AbT, *AtT;      // transposed wall-normal coefficients: AbT[k] = At[k-1], AtT[k] = Ab[k+1]
     double* tape_u1;        // when set, one_step copies the post-inflow velocities here (3 x vol)
+    unsigned char* conv_bits;  // frozen-branch record of this step (vol bytes), with conv_bits_mode
+    int conv_bits_mode;        // TBL_BRANCH_*
     tbl::AdjTape* adj;
     std::vector<double> x1h;  // host copy of x1
     // kernel-group timing (tbl_profile)

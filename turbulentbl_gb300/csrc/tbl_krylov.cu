@@ -385,18 +385,27 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
 }
 
 // New row of L (row nv-1: <v_{nv-1}, v_j>, j < nv-1), then (I + L) t = d by
-// forward substitution into the Hessenberg column.  Rows of older vectors
-// were written when each was the newest.
-__global__ void k_lsg_solve(int K1, int nv, double* __restrict__ Lm, const double* __restrict__ d,
-                            const double* __restrict__ gnew, double* __restrict__ hcol) {
-    if (threadIdx.x != 0) return;
-    const int r = nv - 1;
-    for (int j = 0; j < r; ++j) Lm[(size_t)r * K1 + j] = gnew[j];
-    for (int i = 0; i < nv; ++i) {
-        double t = d[i];
-        for (int j = 0; j < i; ++j) t -= Lm[(size_t)i * K1 + j] * hcol[j];
-        hcol[i] = t;
+// column-oriented forward substitution in shared memory, one warp (nv <= 64:
+// each lane owns rows lane and lane+32).  Rows of older vectors were written
+// when each was the newest.
+__global__ void __launch_bounds__(32) k_lsg_solve(int K1, int nv, double* __restrict__ Lm,
+                                                  const double* __restrict__ d, const double* __restrict__ gnew,
+                                                  double* __restrict__ hcol) {
+    __shared__ double sL[64][65];
+    __shared__ double st[64];
+    const int lane = threadIdx.x, r = nv - 1;
+    for (int j = lane; j < r; j += 32) Lm[(size_t)r * K1 + j] = gnew[j];
+    __syncwarp();
+    for (int i = 0; i < nv; ++i)
+        for (int j = lane; j < i; j += 32) sL[i][j] = i == r ? gnew[j] : Lm[(size_t)i * K1 + j];
+    for (int i = lane; i < nv; i += 32) st[i] = d[i];
+    __syncwarp();
+    for (int j = 0; j < nv; ++j) {
+        const double tj = st[j];  // final: every earlier column has been applied
+        for (int i = j + 1 + lane; i < nv; i += 32) st[i] -= sL[i][j] * tj;
+        __syncwarp();
     }
+    for (int i = lane; i < nv; i += 32) hcol[i] = st[i];
 }
 
 // w -= sum_i t_i v_i (FP32), then ||w|| -> *out (sqrt of the deterministic sum)
@@ -435,7 +444,7 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
     k_lsg_dots_f<<<grid, RED_THREADS, 0, h->stream>>>(n4, (const float4*)W, (const float4*)h->Vf, n4, kit,
                                                       h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d,
                                                       h->lsg_g);
-    k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);
+    k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);  // kit <= 63
     k_lsg_update_f<<<nb, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
                                                       &hcol[kit]);
     h->launches += 3;

@@ -175,6 +175,112 @@ __global__ void __launch_bounds__(128) k_conv_q(Geom g, ConvCoef<T> c, const T* 
     Q3[p] = q7 - (c.dt * g3);
 }
 
+// ------------------------------------------ frozen-branch convection (FP64)
+// The same convection + explicit RHS with its data-dependent decisions
+// either recorded (BM = 1) or taken from a record (BM = 2) instead of from the
+// current field: used by adjoint windows to make finite differences follow
+// the branch decisions the adjoint differentiates.  One byte per point:
+// bits 0-2 the x/y/z Peclet windows, bit 3 u >= 0, bit 4 v >= 0, bit 5 v <= 0,
+// bit 6 w >= 0.  With BM = 1 every value is bitwise that of k_conv_q.
+__device__ __forceinline__ unsigned conv_decide(double u, double v, double w, double dz, const ConvCoef<double>& c) {
+    unsigned b = 0;
+    double s = u > -1.0 ? 1.0 : -1.0;
+    double Pe = s * c.tf * u * c.dx;
+    if (Pe > 2.0 && Pe < 50.0) b |= 1u;
+    s = v > -1.0 ? 1.0 : -1.0;
+    Pe = s * c.tf * v * c.dy;
+    if (Pe > 2.0 && Pe < 50.0) b |= 2u;
+    s = w > -1.0 ? 1.0 : -1.0;
+    Pe = (s * c.tf * w * dz);
+    if (Pe > 2.0 && Pe < 5.0) b |= 4u;
+    if (u >= 0.0) b |= 8u;
+    if (v >= 0.0) b |= 16u;
+    if (v <= 0.0) b |= 32u;
+    if (w >= 0.0) b |= 64u;
+    return b;
+}
+
+// x and xi: central (near the ends), windowed dissipative, or 4th-order central
+__device__ __forceinline__ double conv_fxz(double m, bool nearb, bool win, bool pos, double fm2, double fm1, double f0,
+                                          double fp1, double fp2, double near_c, double q25, double c12) {
+    if (nearb) return m * (fp1 - fm1) * near_c;
+    if (win) {
+        const double a = pos ? m : -m;
+        double t1 = a * (fp2 - 4.0 * fp1 + 6.0 * f0 - 4.0 * fm1 + fm2) * q25;
+        double t2 = m * (-fp2 + 8.0 * fp1 - 8.0 * fm1 + fm2) * c12;
+        return t1 + t2;
+    }
+    return m * ((fm2 - 8.0 * fm1 + 8.0 * fp1 - fp2) * c12);
+}
+
+__device__ __forceinline__ double conv_fy(double v, bool nearb, bool win, bool vp, bool vn, double fm2, double fm1,
+                                         double f0, double fp1, double fp2, const ConvCoef<double>& c) {
+    if (nearb) {
+        const double a1 = vp ? v : 0.0, b = vn ? v : 0.0;
+        return a1 * ((f0 - fm1) * c.invdy) + b * ((fp1 - f0) * c.invdy);
+    }
+    if (win) {
+        const double a = vp ? v : -v;
+        double t1 = a * (fp2 - 4.0 * fp1 + 6.0 * f0 - 4.0 * fm1 + fm2) * c.q25y;
+        double t2 = v * (-fp2 + 8.0 * fp1 - 8.0 * fm1 + fm2) * c.c12y;
+        return t1 + t2;
+    }
+    return v * ((fm2 - 8.0 * fm1 + 8.0 * fp1 - fp2) * c.c12y);
+}
+
+template <int BM>
+__global__ void __launch_bounds__(128) k_conv_q_br(Geom g, ConvCoef<double> c, const double* __restrict__ U1,
+                                                   const double* __restrict__ U2, const double* __restrict__ U3,
+                                                   const double* __restrict__ Pr, const double* __restrict__ x3,
+                                                   const double* __restrict__ jacinv, double* __restrict__ Q1,
+                                                   double* __restrict__ Q2, double* __restrict__ Q3,
+                                                   unsigned char* __restrict__ bits) {
+    int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    if (i > g.nx - 2) return;
+    const long long p = idx(g, i, j, k);
+    const long long sz = g.ps;
+    const int ja = jm1(g, j), jb = jm2(g, j), jc = jp1(g, j), jd = jp2(g, j);
+    const long long pjm1 = idx(g, i, ja, k), pjm2 = idx(g, i, jb, k), pjp1 = idx(g, i, jc, k),
+                    pjp2 = idx(g, i, jd, k);
+    const bool nbx = (i <= 1) || (i >= g.nx - 2);
+    const bool nby = (j == 1) || (j == g.ny - 2);
+    const bool nbz = (k <= 1) || (k >= g.nz - 2);
+    const double u = U1[p], v = U2[p], w = U3[p];
+    const double dz = (x3[k + 1] - x3[k]);
+    const double jk = jacinv[k];
+    unsigned b;
+    if (BM == 2) {
+        b = bits[p];
+    } else {
+        b = conv_decide(u, v, w, dz, c);
+        bits[p] = (unsigned char)b;
+    }
+    const bool wx = b & 1u, wy = b & 2u, wz = b & 4u, up = b & 8u, vp = b & 16u, vn = b & 32u, wp = b & 64u;
+    const double* Fs[3] = {U1, U2, U3};
+    double conv[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+        const double* F = Fs[cc];
+        double f0 = F[p];
+        double d1 = conv_fxz(u, nbx, wx, up, nbx ? 0.0 : F[p - 2], F[p - 1], f0, F[p + 1], nbx ? 0.0 : F[p + 2],
+                             c.inv2dx, c.q25x, c.c12x);
+        double d2 = conv_fy(v, nby, wy, vp, vn, F[pjm2], F[pjm1], f0, F[pjp1], F[pjp2], c);
+        double d3 = conv_fxz(w, nbz, wz, wp, nbz ? 0.0 : F[p - 2 * sz], F[p - sz], f0, F[p + sz],
+                             nbz ? 0.0 : F[p + 2 * sz], c.h05z, c.q25z, c.c12z);
+        conv[cc] = d1 + d2 + (d3 * jk);
+    }
+    double g1 = 0.5 * (Pr[p + 1] - Pr[p - 1]) * c.invdx;
+    double g2 = 0.5 * (Pr[pjp1] - Pr[pjm1]) * c.invdy;
+    double g3 = 0.5 * (Pr[p + sz] - Pr[p - sz]) * (c.invdxi * jk);
+    double q5 = u + (c.dt * (0.0 - conv[0]));
+    Q1[p] = q5 - (c.dt * g1);
+    double q6 = v + (c.dt * (0.0 - conv[1]));
+    Q2[p] = q6 - (c.dt * g2);
+    double q7 = w + (c.dt * (0.0 - conv[2]));
+    Q3[p] = q7 - (c.dt * g3);
+}
+
 // ---------------------------------------------------------- GS residual
 // L1 norm of the residual of (1 - dt/Re L7) U = Q over all slabs' interiors,
 // with current (global) halos (dnstbl2/dnstbl.f90:781-828).  blockIdx.y picks
@@ -700,6 +806,14 @@ int launch_conv_q(tbl_handle* h) {
         k_conv_q<float><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<float>(h->cfg), h->Uf[0], h->Uf[1],
                                                                  h->Uf[2], h->Pf, h->x3, h->jacinv, h->Qf[0],
                                                                  h->Qf[1], h->Qf[2]);
+    else if (h->conv_bits_mode == TBL_BRANCH_RECORD && h->conv_bits)
+        k_conv_q_br<1><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<double>(h->cfg), h->U[0], h->U[1],
+                                                                 h->U[2], h->Pr, h->x3, h->jacinv, h->Q[0], h->Q[1],
+                                                                 h->Q[2], h->conv_bits);
+    else if (h->conv_bits_mode == TBL_BRANCH_REPLAY && h->conv_bits)
+        k_conv_q_br<2><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<double>(h->cfg), h->U[0], h->U[1],
+                                                                 h->U[2], h->Pr, h->x3, h->jacinv, h->Q[0], h->Q[1],
+                                                                 h->Q[2], h->conv_bits);
     else
         k_conv_q<double><<<interior_grid(g), 128, 0, h->stream>>>(g, conv_coef<double>(h->cfg), h->U[0], h->U[1],
                                                                   h->U[2], h->Pr, h->x3, h->jacinv, h->Q[0], h->Q[1],

@@ -70,9 +70,9 @@ class TblGpu(AbiRunner):
         if st != abi.TBL_OK:
             raise TblError(st, "tbl_set_wall_control")
 
-    def forward_window(self, nsteps, x_lo, x_hi, ckpt_every):
+    def forward_window(self, nsteps, x_lo, x_hi, ckpt_every, branch_mode=abi.TBL_BRANCH_FREE):
         """Run nsteps recorded steps; returns (objective, per-step stats dicts)."""
-        wc = abi.TblWindowConfig(x_lo, x_hi, int(ckpt_every), 0)
+        wc = abi.TblWindowConfig(x_lo, x_hi, int(ckpt_every), int(branch_mode))
         J = C.c_double(0.0)
         stats = (abi.TblStepStats * nsteps)()
         st = self.lib.tbl_forward_window(self._h, int(nsteps), C.byref(wc), C.byref(J), stats)
