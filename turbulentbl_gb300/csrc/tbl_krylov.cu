@@ -241,6 +241,7 @@ __global__ void k_update_f(long long n4, double* __restrict__ pc, const float4* 
                            const double* __restrict__ gy, int kit) {
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
         for (int i = 0; i < kit; ++i) {
             const float4 v = V[(long long)i * vstride4 + q];
             const float y = (float)gy[i];
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(32) k_lsg_solve(int K1, int nv, double* __rest
 }
 
 // w -= sum_i t_i v_i (FP32), then ||w|| -> *out (sqrt of the deterministic sum)
-__global__ void __launch_bounds__(RED_THREADS, 8) k_lsg_update_f(long long n4, float4* __restrict__ w,
+__global__ void __launch_bounds__(RED_THREADS, 6) k_lsg_update_f(long long n4, float4* __restrict__ w,
                                                               const float4* __restrict__ V, long long vstride4, int nv,
                                                               const double* __restrict__ t, RedWork rw, int slot,
                                                               double* out) {
@@ -420,6 +421,7 @@ __global__ void __launch_bounds__(RED_THREADS, 8) k_lsg_update_f(long long n4, f
     double acc = 0.0;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
         float4 x = w[q];
+#pragma unroll 4
         for (int i = 0; i < nv; ++i) {
             const float4 v = V[(long long)i * vstride4 + q];
             const float ti = s_t[i];
@@ -440,12 +442,19 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
     if (kit > 64 || kit > K1) return TBL_ERR_BAD_ARG;
     const int nb = red_blocks(h);
     const long long n4 = h->g.vol / 4;
-    dim3 grid(nb, (kit + LSG_G - 1) / LSG_G);
+    // dot pass: the groups together fill one resident wave (3 blocks of 256 per SM at its register use)
+    const int ngr = (kit + LSG_G - 1) / LSG_G;
+    int nbd = (3 * (h->n_sm > 0 ? h->n_sm : 148)) / ngr;
+    if (nbd < 1) nbd = 1;
+    if (nbd > nb) nbd = nb;
+    dim3 grid(nbd, ngr);
     k_lsg_dots_f<<<grid, RED_THREADS, 0, h->stream>>>(n4, (const float4*)W, (const float4*)h->Vf, n4, kit,
                                                       h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d,
                                                       h->lsg_g);
     k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);  // kit <= 63
-    k_lsg_update_f<<<nb, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
+    int nbu = 6 * (h->n_sm > 0 ? h->n_sm : 148);  // one resident wave at 6 blocks per SM
+    if (nbu > nb) nbu = nb;
+    k_lsg_update_f<<<nbu, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
                                                       &hcol[kit]);
     h->launches += 3;
     return TBL_OK;
