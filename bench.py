@@ -175,6 +175,8 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     torch.cuda.set_device(local)
     from turbulentbl_gb300.lib import TblGpu
     mesh, rp, st = make_state(wl, nproc=nproc)
+    if wl.precision == abi.TBL_PREC_MIXED:
+        rp.flags |= abi.TBL_FLAG_PPE_RESIDUAL  # the true ||L7 p' - Q8|| / ||Q8|| every step (one extra pass)
     g = TblGpu(mesh, rp)
     g.upload(st)
     for _ in range(warmup):
@@ -210,6 +212,10 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launch_groups": nl[q]} for q in range(ng - 1)}
     out = {"elapsed": elapsed, "host_elapsed": e1 - e0, "recs": recs, "status": st_all, "launches": launches,
            "clocks": clk, "groups": groups}
+    if wl.precision == abi.TBL_PREC_MIXED:
+        out["mixed_state"] = g.download(fields=("u", "v", "w", "p"))
+        out["mixed_stats"] = g.download_stats()
+        out["accuracy_steps"] = warmup + steps
     if do_e2e:
         nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
         n = nx * ny * nz
@@ -239,9 +245,36 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
         out["e2e"] = {"elapsed": te, "h2d": 5 * n * 8, "d2h": 4 * n * 8,
                       "iters": [r["gmres_iters"] for r in e2e_recs]}
     g.close()
+    if "mixed_state" in out and rank == 0:
+        out["accuracy"] = mixed_accuracy(wl, nproc, out.pop("mixed_state"), out.pop("mixed_stats"),
+                                         out["accuracy_steps"], out["recs"])
     if do_cpu and rank == 0:
         out["cpu"] = run_cpu(wl, nproc, cpu_budget, 1)
     return out
+
+
+def mixed_accuracy(wl, nproc, dm, sm, nsteps, recs):
+    """The mixed-precision state after nsteps steps against the FP64 library
+    (which matches the FP64 oracle to 1e-12) from the same seeded start:
+    per-field relative L2, the mean streamwise-velocity profile U(y) and the
+    running statistics, plus the worst true PPE residual of the timed steps."""
+    from turbulentbl_gb300.lib import TblGpu
+    mesh, rp, st = make_state(wl, nproc=nproc)
+    rp.precision = abi.TBL_PREC_FP64
+    g = TblGpu(mesh, rp)
+    g.upload(st)
+    g.step(nsteps, check=False)
+    d = g.download(fields=("u", "v", "w", "p"))
+    s64 = g.download_stats()
+    g.close()
+    rel = {f: float(np.linalg.norm(dm[f] - d[f]) / np.linalg.norm(d[f])) for f in ("u", "v", "w", "p")}
+    prof = lambda u: u[1:-1, 1:-1, :].mean(axis=(0, 1))  # mean over x and span at each wall distance
+    p64, pm = prof(d["u"]), prof(dm["u"])
+    us64, usm = s64["usum"][1:-1, 1:-1], sm["usum"][1:-1, 1:-1]
+    return {"steps_compared": nsteps, "rel_l2": rel,
+            "mean_profile_max_rel": float(np.abs(pm - p64).max() / np.abs(p64).max()),
+            "usum_max_rel": float(np.abs(usm - us64).max() / max(np.abs(us64).max(), 1e-300)),
+            "ppe_rel_resid_max": max(r["ppe_rel_resid"] for r in recs)}
 
 
 def run_adjoint(wl, nproc, window, ckpt, n_fd, local):
@@ -404,6 +437,8 @@ def main():
         line["e2e"] = {"value": whole_job_rate(wl.points, K, world, e["elapsed"]), "unit": "Mpt-steps/s",
                        "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"],
                        "gmres_iters_per_step": e["iters"]}
+    if "accuracy" in r:
+        line["accuracy_vs_fp64"] = r["accuracy"]
     if "cpu" in r:
         c = r["cpu"]
         line["cpu_baseline"] = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")}

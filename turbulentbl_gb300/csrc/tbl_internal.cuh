@@ -95,6 +95,8 @@ struct tbl_handle {
     double* Q[3];
     double* Q8;
     double* RH;      // SSOR forward result (scaled)
+    double* PRE;     // 3 x vol: old-value terms of the GS point updates (FP64)
+    float* PREf;     // 3 x vol: the same in mixed precision
     double* V;       // kmax+1 Krylov vectors, vol each
     double* uold1;   // U1 at i=1 before the inflow update, (ny, nz)
     // mixed precision (TBL_PREC_MIXED): FP32 fields and inner-GMRES vectors

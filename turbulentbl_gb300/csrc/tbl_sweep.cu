@@ -48,6 +48,7 @@ struct SweepArgs {
     double t;                   // -dt/Re
     T* F[3];
     const T* Q[3];
+    const T* PRE[3];            // per-point terms of old values (k_gs_pre)
     int comp[3];
     const T* halo_in;           // [comp][side][slab] planes
     T* halo_out;
@@ -191,21 +192,19 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         ckd = wr * (MODE == SW_FWD ? a.Ab[k] : a.At[k]);
         cid = wr * a.aw;
     }
-    const Val p0 = (Val)c0, p1 = (Val)c1, p2 = (Val)c2, p3 = (Val)c3, cj = (Val)cjd, ck = (Val)ckd, ci = (Val)cid;
+    const Val p0 = (Val)c0, p2 = (Val)c2, cj = (Val)cjd, ck = (Val)ckd, ci = (Val)cid;
+    (void)c1;
+    (void)c3;
 
     // line pointers (physical chunk c at element CH*c)
     Val* F = MODE == SW_GS ? a.F[comp] + line : nullptr;
-    const Val* Qc = MODE == SW_GS ? a.Q[comp] + line : nullptr;
     const Val* Fjp = MODE == SW_GS ? a.F[comp] + sy * ((long long)jp + (long long)g.ny * k) : nullptr;
-    const Val* Fkp = nullptr;
     const Val* kin = nullptr;  // plane below (global): warp 0 across CTAs, slab edge
     const Val* jin = nullptr;  // row above (global): lane 0
     bool kin_zero = false, jin_zero = false;
     Val* hout = nullptr;  // GS: next sweep's halo copy of this plane
     if (MODE == SW_GS) {
         const size_t hp = (size_t)g.ps, base = (size_t)comp * 2 * a.P;
-        Fkp = (kidx == K - 1 && cta.slab < a.P - 1) ? a.halo_in + (base + 1 * a.P + cta.slab) * hp + sy * j
-                                                    : a.F[comp] + line + g.ps;
         kin = (kidx == 0 && cta.slab > 0) ? a.halo_in + (base + 0 * a.P + cta.slab) * hp + sy * j
                                           : a.F[comp] + line - g.ps;
         jin = a.F[comp] + sy * ((long long)jm + (long long)g.ny * k);
@@ -219,7 +218,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         jin = io + sy * ((long long)(jin_zero ? j : (MODE == SW_FWD ? j - 1 : j + 1)) + (long long)g.ny * k);
     }
     Val* outp = MODE == SW_GS ? F : (MODE == SW_FWD ? a.RH : a.OUT) + line;
-    const Val* inp = MODE == SW_GS ? nullptr : a.RH + line;
+    const Val* inp = MODE == SW_GS ? a.PRE[comp] + line : a.RH + line;
     const bool wrap = MODE == SW_GS && jp == 1;  // the row after j holds new values (periodic GS)
 
     Val last[CH];
@@ -229,47 +228,26 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     long long seen_j = -1, seen_k = -1;
 
     // raw operands loaded one step ahead
-    Val ra[CH], rb[CH], rc[CH], rd_[CH];
-    Val rnx = Val(0);
+    Val ra[CH];
+    // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
+    // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
     auto load_raw = [&](int ts) {
         const int cl = ts - jl - kl;
         if (!line_ok || cl < 0 || cl >= C) return;
         const int i0 = CH * (MODE == SW_BWD ? C - 1 - cl : cl);
-        if (MODE == SW_GS) {
 #pragma unroll
-            for (int e = 0; e < CH; ++e) { ra[e] = Qc[i0 + e]; rb[e] = F[i0 + e]; }
-            rnx = (i0 + CH - 1 <= g.nx - 2) ? F[i0 + CH] : Val(0);
-            if (!wrap) {
-#pragma unroll
-                for (int e = 0; e < CH; ++e) rc[e] = __ldcg(Fjp + i0 + e);
-            }
-#pragma unroll
-            for (int e = 0; e < CH; ++e) rd_[e] = __ldcg(Fkp + i0 + e);
-        } else {
-#pragma unroll
-            for (int e = 0; e < CH; ++e) ra[e] = inp[i0 + e];
-        }
+        for (int e = 0; e < CH; ++e) ra[e] = inp[i0 + e];
     };
     Val pre[CH];
     auto make_pre = [&](int ts) {
         const int cl = ts - jl - kl;
         if (!line_ok || cl < 0 || cl >= C) return;
-        if (MODE == SW_GS) {
 #pragma unroll
-            for (int e = 0; e < CH; ++e) {
-                Val oip = e < CH - 1 ? rb[e + 1] : rnx;
-                Val x = fma(p1, oip, p0 * ra[e]);
-                if (!wrap) x = fma(p2, rc[e], x);
-                pre[e] = fma(p3, rd_[e], x);
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < CH; ++e) pre[e] = p0 * ra[e];
-        }
+        for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
     };
     load_raw(T0);
     make_pre(T0);
-    Val bnd = MODE == SW_GS ? rb[0] : Val(0);  // GS: U(0) of the first chunk
+    const Val bnd = MODE == SW_GS ? F[0] : Val(0);  // GS: U(0), the inflow boundary value of the line
     Val pj_pf[CH], pk_pf[CH];
     bool pj_ok = false, pk_ok = false;
     int abort = 0;
@@ -415,18 +393,58 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             }
         }
         make_pre(T + 1);
-        if (MODE == SW_GS) bnd = rb[0];
     }
     (void)tend_j;
 }
 
+// The part of a Gauss-Seidel point update that reads only values the sweep
+// has not yet replaced (Q, U(i+1), U(j+1) except on the periodic wrap row,
+// U(k+1) or the slab's halo snapshot), in the sweep's reassociated form and
+// FMA order: PRE = fma(p3, U(k+1), fma(p2, U(j+1), fma(p1, U(i+1), p0 Q))).
+// Fully parallel, so the wavefront sweep keeps only the three FMAs that
+// depend on new values.  blockIdx.z runs over (component, plane).
+template <typename T>
+struct Ptr3 {
+    const T* p[3];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gs_pre(Geom g, double t, double aw_, double as_,
+                                                const double* __restrict__ Ap, const double* __restrict__ At,
+                                                const int* __restrict__ slab_of_k,
+                                                const SlabDesc* __restrict__ slabs, int P, int c0_, int c1_, int c2_,
+                                                Ptr3<T> Fs, Ptr3<T> Qs, Ptr3<T> PREs,
+                                                const T* __restrict__ halo_in) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y;
+    const int K = g.nz - 2;
+    const int ci = blockIdx.z / K, k = 1 + blockIdx.z % K;
+    if (i > g.nx - 2) return;
+    const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
+    const T* F = Fs.p[comp];
+    const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
+    const double rd = 1.0 / (1.0 + (t * Ap[k]));
+    const T p0 = (T)rd, p1 = (T)(-(t * aw_) * rd), p2 = (T)(-(t * as_) * rd), p3 = (T)(-(t * At[k]) * rd);
+    const int jp = (j == g.ny - 2) ? 1 : j + 1;
+    const int r = slab_of_k[k];
+    const SlabDesc sl = slabs[r];
+    const T* Fkp = (k == sl.bn + sl.K - 1 && r < P - 1)
+                       ? halo_in + ((size_t)comp * 2 * P + 1 * P + r) * (size_t)g.ps + (size_t)g.sx * j
+                       : F + line + g.ps;
+    T x = fma(p1, F[line + i + 1], p0 * Qs.p[comp][line + i]);
+    if (jp != 1) x = fma(p2, F[(long long)g.sx * ((long long)jp + (long long)g.ny * k) + i], x);
+    const_cast<T*>(PREs.p[comp])[line + i] = fma(p3, Fkp[i], x);
+}
+
 // r = L7 X (Q8 == nullptr) or r = Q8 - L7 X on the interior, written to R
 // (:1001-1006 restart residual, :1098-1101 Arnoldi matvec), global halos.
+// With rAp non-null the result is multiplied by the forward sweep's
+// coefficient -w/Ap(k) (rounded to the sweep's type first, as the sweep did).
 template <typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(256) k_lap(Geom g, double aw_, double as_, const double* __restrict__ Ab,
                                              const double* __restrict__ At, const double* __restrict__ Ap,
                                              const TI* __restrict__ X, const double* __restrict__ Q8,
-                                             TO* __restrict__ R) {
+                                             TO* __restrict__ R, double omega, const double* __restrict__ rAp) {
     const TC aw = (TC)aw_, as = (TC)as_;
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
@@ -437,7 +455,8 @@ __global__ void __launch_bounds__(256) k_lap(Geom g, double aw_, double as_, con
     const TC xjp = (TC)X[(long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k)];
     TC lap = aw * (TC)X[p - 1] + aw * (TC)X[p + 1] + as * xjm + as * xjp + (TC)Ab[k] * (TC)X[p - g.ps] +
              (TC)At[k] * (TC)X[p + g.ps] + (TC)Ap[k] * (TC)X[p];
-    R[p] = (TO)(Q8 ? ((TC)Q8[p] - (lap)) : lap);
+    const TO r = (TO)(Q8 ? ((TC)Q8[p] - (lap)) : lap);
+    R[p] = rAp ? (TO)(-omega * rAp[k]) * r : r;
 }
 
 // ------------------------------------------------------------- host glue
@@ -504,31 +523,47 @@ static int launch_sweep(tbl_handle* h, SweepArgs<T>& a, int ncomp) {
     return TBL_OK;
 }
 
-// GS sweep for the listed components; halo buffers ping-pong by `parity`.
-int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity) {
+template <typename T>
+static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T* const PRE[3], T* halo,
+                            const int* comps, int ncomp, int parity) {
     const size_t hsz = (size_t)3 * 2 * h->P * h->g.ps;
-    if (h->cfg.precision == TBL_PREC_MIXED) {  // delta form: iterate on D with r0 in Qf
-        SweepArgs<float> a = base_args<float>(h);
-        for (int c = 0; c < 3; ++c) { a.F[c] = h->Df[c]; a.Q[c] = h->Qf[c]; }
-        for (int c = 0; c < ncomp; ++c) a.comp[c] = comps[c];
-        float* hf = reinterpret_cast<float*>(h->halo);
-        a.halo_in = hf + (size_t)(parity & 1) * hsz;
-        a.halo_out = hf + (size_t)((parity + 1) & 1) * hsz;
-        return launch_sweep<SW_GS, float>(h, a, ncomp);
-    }
-    SweepArgs<double> a = base_args<double>(h);
-    for (int c = 0; c < 3; ++c) { a.F[c] = h->U[c]; a.Q[c] = h->Q[c]; }
+    SweepArgs<T> a = base_args<T>(h);
+    for (int c = 0; c < 3; ++c) { a.F[c] = F[c]; a.Q[c] = Q[c]; a.PRE[c] = PRE[c]; }
     for (int c = 0; c < ncomp; ++c) a.comp[c] = comps[c];
-    a.halo_in = h->halo + (size_t)(parity & 1) * hsz;
-    a.halo_out = h->halo + (size_t)((parity + 1) & 1) * hsz;
-    return launch_sweep<SW_GS, double>(h, a, ncomp);
+    a.halo_in = halo + (size_t)(parity & 1) * hsz;
+    a.halo_out = halo + (size_t)((parity + 1) & 1) * hsz;
+    const Geom& g = h->g;
+    Ptr3<T> Fs, Qs, Ps;
+    for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; Ps.p[c] = PRE[c]; }
+    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
+    k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, a.t, a.aw, a.as, h->Ap, h->At, h->slab_of_k, h->slabs, h->P,
+                                             comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0, Fs, Qs,
+                                             Ps, a.halo_in);
+    h->launches++;
+    return launch_sweep<SW_GS, T>(h, a, ncomp);
+}
+
+// GS sweep for the listed components (old-value terms precomputed first);
+// halo buffers ping-pong by `parity`.
+int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity) {
+    if (h->cfg.precision == TBL_PREC_MIXED) {  // delta form: iterate on D with r0 in Qf
+        float* F[3] = {h->Df[0], h->Df[1], h->Df[2]};
+        const float* Q[3] = {h->Qf[0], h->Qf[1], h->Qf[2]};
+        float* P[3] = {h->PREf, h->PREf + h->g.vol, h->PREf + 2 * h->g.vol};
+        return gs_pre_and_sweep<float>(h, F, Q, P, reinterpret_cast<float*>(h->halo), comps, ncomp, parity);
+    }
+    double* F[3] = {h->U[0], h->U[1], h->U[2]};
+    const double* Q[3] = {h->Q[0], h->Q[1], h->Q[2]};
+    double* P[3] = {h->PRE, h->PRE + h->g.vol, h->PRE + 2 * h->g.vol};
+    return gs_pre_and_sweep<double>(h, F, Q, P, h->halo, comps, ncomp, parity);
 }
 
 // Forward SSOR sweep of r = L7 X (Q8 == nullptr) or r = Q8 - L7 X.
 int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
     const Geom& g = h->g;
     k_lap<double, double, double><<<dim3((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2), 256, 0, h->stream>>>(
-        g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH);
+        g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
+        h->cfg.omega, h->rAp);
     h->launches++;
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
@@ -549,9 +584,11 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
     dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
     const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
     if (PCd)
-        k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf);
+        k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf,
+                                                                  h->cfg.omega, h->rAp);
     else
-        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, Xf, nullptr, h->RHf);
+        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, Xf, nullptr, h->RHf,
+                                                                h->cfg.omega, h->rAp);
     h->launches++;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
