@@ -116,7 +116,7 @@ static void free_all(tbl_handle* h) {
     for (void* p : mptrs)
         if (p) cudaFree(p);
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
-                    h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->usum2, h->vsum2,
+                    h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->gs_coef, h->usum2, h->vsum2,
                     h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
                     h->usum2_fl, h->sums, h->bl_out, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
                     h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
@@ -185,6 +185,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->x3, (size_t)nz)); TRY(dalloc(&h->jacinv, (size_t)nz)); TRY(dalloc(&h->jac2, (size_t)nz));
     TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
     TRY(dalloc(&h->rAp, (size_t)nz));
+    TRY(dalloc(&h->gs_coef, 4 * (size_t)nz));
     TRY(dalloc(&h->usum2, n2)); TRY(dalloc(&h->vsum2, n2)); TRY(dalloc(&h->wsum2, n2)); TRY(dalloc(&h->wt, n2));
     TRY(dalloc(&h->ume1, (size_t)nz)); TRY(dalloc(&h->bltkns, (size_t)nx)); TRY(dalloc(&h->newk, (size_t)nz));
     TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));

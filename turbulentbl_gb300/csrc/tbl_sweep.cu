@@ -408,9 +408,21 @@ struct Ptr3 {
     const T* p[3];
 };
 
+// Per-plane coefficients of the reassociated GS update (the values the sweep
+// computes per warp): [p0 | p1 | p2 | p3] x nz.
+__global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double* __restrict__ Ap,
+                          const double* __restrict__ At, double* __restrict__ pc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nz) return;
+    const double rd = 1.0 / (1.0 + (t * Ap[k]));
+    pc[k] = rd;
+    pc[nz + k] = -(t * aw_) * rd;
+    pc[2 * nz + k] = -(t * as_) * rd;
+    pc[3 * nz + k] = -(t * At[k]) * rd;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_gs_pre(Geom g, double t, double aw_, double as_,
-                                                const double* __restrict__ Ap, const double* __restrict__ At,
+__global__ void __launch_bounds__(256) k_gs_pre(Geom g, const double* __restrict__ pc,
                                                 const int* __restrict__ slab_of_k,
                                                 const SlabDesc* __restrict__ slabs, int P, int c0_, int c1_, int c2_,
                                                 Ptr3<T> Fs, Ptr3<T> Qs, Ptr3<T> PREs,
@@ -423,8 +435,8 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, double t, double aw_, do
     const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
     const T* F = Fs.p[comp];
     const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
-    const double rd = 1.0 / (1.0 + (t * Ap[k]));
-    const T p0 = (T)rd, p1 = (T)(-(t * aw_) * rd), p2 = (T)(-(t * as_) * rd), p3 = (T)(-(t * At[k]) * rd);
+    const int nz = g.nz;
+    const T p0 = (T)pc[k], p1 = (T)pc[nz + k], p2 = (T)pc[2 * nz + k], p3 = (T)pc[3 * nz + k];
     const int jp = (j == g.ny - 2) ? 1 : j + 1;
     const int r = slab_of_k[k];
     const SlabDesc sl = slabs[r];
@@ -536,7 +548,7 @@ static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T
     Ptr3<T> Fs, Qs, Ps;
     for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; Ps.p[c] = PRE[c]; }
     dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
-    k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, a.t, a.aw, a.as, h->Ap, h->At, h->slab_of_k, h->slabs, h->P,
+    k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, h->gs_coef, h->slab_of_k, h->slabs, h->P,
                                              comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0, Fs, Qs,
                                              Ps, a.halo_in);
     h->launches++;
@@ -622,6 +634,11 @@ __global__ void k_halo_init(Geom g, const SlabDesc* __restrict__ slabs, int P, c
 
 int launch_halo_init(tbl_handle* h, int parity) {
     const size_t hsz = (size_t)3 * 2 * h->P * h->g.ps;
+    // per-plane GS coefficients of the operator in use (the adjoint swaps in A^T)
+    k_gs_coef<<<(h->g.nz + 127) / 128, 128, 0, h->stream>>>(h->g.nz, -h->cfg.dt / (h->cfg.re),
+                                                             1.0 / (h->cfg.dx * h->cfg.dx),
+                                                             1.0 / (h->cfg.dy * h->cfg.dy), h->Ap, h->At, h->gs_coef);
+    h->launches++;
     if (h->cfg.precision == TBL_PREC_MIXED)
         k_halo_init<float><<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(
             h->g, h->slabs, h->P, h->Df[0], h->Df[1], h->Df[2], reinterpret_cast<float*>(h->halo) + (size_t)(parity & 1) * hsz);
