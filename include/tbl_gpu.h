@@ -80,6 +80,7 @@ typedef struct tbl_config {
     double errorstop;       /* GS L1 residual ratio (reference: 1e-6, :23) */
     double mixed_inner_tol; /* inner FP32 GMRES relative tolerance (mixed mode) */
     double mixed_outer_tol; /* FP64 refinement residual target, relative (mixed mode) */
+    double mixed_true_tol;  /* mixed mode: also refine until ||Q8 - L7 p'||_2 / ||Q8||_2 <= this (0 = off) */
 } tbl_config;
 
 /* Mesh, host-computed once (dnstbl2/dnstbl.f90:392-426): x1(nx), x2(ny),

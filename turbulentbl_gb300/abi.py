@@ -58,7 +58,7 @@ class TblConfig(C.Structure):
         ("dt", C.c_double), ("re", C.c_double), ("ue", C.c_double),
         ("dx", C.c_double), ("dy", C.c_double), ("dxi", C.c_double),
         ("omega", C.c_double), ("errtol", C.c_double), ("errorstop", C.c_double),
-        ("mixed_inner_tol", C.c_double), ("mixed_outer_tol", C.c_double),
+        ("mixed_inner_tol", C.c_double), ("mixed_outer_tol", C.c_double), ("mixed_true_tol", C.c_double),
     ]
 
 

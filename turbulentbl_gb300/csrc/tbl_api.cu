@@ -185,7 +185,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->x3, (size_t)nz)); TRY(dalloc(&h->jacinv, (size_t)nz)); TRY(dalloc(&h->jac2, (size_t)nz));
     TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
     TRY(dalloc(&h->rAp, (size_t)nz));
-    TRY(dalloc(&h->gs_coef, 4 * (size_t)nz));
+    TRY(dalloc(&h->gs_coef, 7 * (size_t)nz));
     TRY(dalloc(&h->usum2, n2)); TRY(dalloc(&h->vsum2, n2)); TRY(dalloc(&h->wsum2, n2)); TRY(dalloc(&h->wt, n2));
     TRY(dalloc(&h->ume1, (size_t)nz)); TRY(dalloc(&h->bltkns, (size_t)nx)); TRY(dalloc(&h->newk, (size_t)nz));
     TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));
@@ -313,13 +313,23 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
     const int kmax = h->cfg.mixed_kmax, K1 = kmax + 1;
     const size_t vol = (size_t)h->g.vol;
     const double outer_tol = h->cfg.mixed_outer_tol, inner_tol = h->cfg.mixed_inner_tol;
-    double sumav = 1.0, sumnor = 0.0;
+    const double true_tol = h->cfg.mixed_true_tol;
+    double sumav = 1.0, sumnor = 0.0, true_rel = 0.0;
     int m = 0, iters = 0;
     int status = TBL_OK;
+    bool done = false, true_fresh = false;
     const double wN = 4.0 * h->npts;
-    while (sumav > outer_tol && m < h->cfg.mixed_max_outer) {
+    while (!done && m < h->cfg.mixed_max_outer) {
         m = m + 1;
         float* V0 = h->Vf;
+        if (true_tol > 0.0 && !true_fresh) {  // true relative residual of the current p' (FP64)
+            {
+                ProfScope ps(h, TBL_PROF_VEC, 2.0 * 8.0 * h->npts);
+                TRY(launch_ppe_resid(h));
+            }
+            TRY(readback(h, &h->sc->red[9], 2 * sizeof(double)));
+            true_rel = h->hpin[1] > 0 ? std::sqrt(h->hpin[0] / h->hpin[1]) : 0.0;
+        }
         {
             ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN + 2.0 * 8.0 * h->npts);
             TRY(launch_ssor_fwd_f(h, nullptr, h->PC, h->Q8));
@@ -340,13 +350,18 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
             sumnor = rho_m;
         }
         sumav = h->hpin[2];
-        if (sumav <= outer_tol) { kits.push_back(0); break; }
+        const bool true_ok = true_tol <= 0.0 || true_rel <= true_tol;
+        if (sumav <= outer_tol && true_ok) { kits.push_back(0); done = true; break; }
+        // this pass's target for the preconditioned residual: the outer
+        // tolerance, tightened in proportion when the true residual is short
+        double target = outer_tol;
+        if (!true_ok) target = std::fmin(outer_tol, 0.5 * sumav * (true_tol / true_rel));
         {
             ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
             TRY(launch_scale_by_inv_f(h, V0, &h->sc->rho));
         }
         int kit = 0;
-        while (kit < kmax && sumav > outer_tol && sumav * sumnor > inner_tol * rho_m) {
+        while (kit < kmax && sumav > target && sumav * sumnor > inner_tol * rho_m) {
             kit = kit + 1;
             float* W = h->Vf + (size_t)kit * vol;
             {
@@ -381,12 +396,29 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
             ProfScope ps(h, TBL_PROF_VEC, (kit * 4.0 + 16.0) * h->npts);
             TRY(launch_backsub_update_f(h, kit));
         }
+        // the cycle's residual estimate reached its target: accept, after
+        // checking the true residual when that criterion is on
+        true_fresh = false;
+        if (sumav <= target) {
+            if (true_tol > 0.0) {
+                {
+                    ProfScope ps(h, TBL_PROF_VEC, 2.0 * 8.0 * h->npts);
+                    TRY(launch_ppe_resid(h));
+                }
+                TRY(readback(h, &h->sc->red[9], 2 * sizeof(double)));
+                true_rel = h->hpin[1] > 0 ? std::sqrt(h->hpin[0] / h->hpin[1]) : 0.0;
+                true_fresh = true;
+                done = sumav <= outer_tol && true_rel <= true_tol;
+            } else {
+                done = sumav <= outer_tol;
+            }
+        }
     }
     st.gmres_restarts = m;
     st.outer_iters = m;
     st.gmres_iters = iters;
     st.gmres_resid = sumav;
-    if (status == TBL_OK && sumav > outer_tol) status = TBL_ERR_NOT_CONVERGED;
+    if (status == TBL_OK && !done) status = TBL_ERR_NOT_CONVERGED;
     return status;
 }
 
@@ -588,7 +620,7 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
     if (cfg->kmax < 1 || cfg->mmax < 1 || !(cfg->dt > 0) || !(cfg->re > 0)) return TBL_ERR_BAD_ARG;
     if (cfg->precision != TBL_PREC_FP64 && cfg->precision != TBL_PREC_MIXED) return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED &&
-        (cfg->mixed_kmax < 1 || cfg->mixed_kmax > 63 || cfg->mixed_max_outer < 1 || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
+        (cfg->mixed_kmax < 1 || cfg->mixed_kmax > 63 || cfg->mixed_max_outer < 1 || !(cfg->mixed_true_tol >= 0) || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
         return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED && (cfg->flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
     int ndev = 0;

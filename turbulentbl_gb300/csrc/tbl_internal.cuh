@@ -97,7 +97,7 @@ struct tbl_handle {
     double* RH;      // SSOR forward result (scaled)
     double* PRE;     // 3 x vol: old-value terms of the GS point updates (FP64)
     float* PREf;     // 3 x vol: the same in mixed precision
-    double* gs_coef; // 4 x nz per-plane coefficients of the GS update
+    double* gs_coef; // 7 x nz per-plane coefficients of the GS update and residual
     double* V;       // kmax+1 Krylov vectors, vol each
     double* uold1;   // U1 at i=1 before the inflow update, (ny, nz)
     // mixed precision (TBL_PREC_MIXED): FP32 fields and inner-GMRES vectors

@@ -289,10 +289,12 @@ struct GsCoef {
     double cE, cW, cN, cS;  // t*Av{e,w,n,s}, t = -dt/Re
 };
 
+// One block per (plane, row) at a time; the per-plane coefficients come from
+// the table k_gs_coef fills at the start of every GS solve ([d|cT|cB] at
+// 4nz..7nz, the same values as 1 + t Ap(k), t At(k), t Ab(k)).  A row's |res|
+// is summed in T, the rows in FP64.
 template <typename T>
-__global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, const double* __restrict__ Ab,
-                                                          const double* __restrict__ At,
-                                                          const double* __restrict__ Ap, double t,
+__global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, const double* __restrict__ pc,
                                                           const T* __restrict__ U0, const T* __restrict__ U1,
                                                           const T* __restrict__ U2, const T* __restrict__ Q0,
                                                           const T* __restrict__ Q1, const T* __restrict__ Q2,
@@ -302,22 +304,23 @@ __global__ void __launch_bounds__(RED_THREADS) k_gs_resid(Geom g, GsCoef gc, con
     const int comp = cid == 0 ? comps.x : (cid == 1 ? comps.y : comps.z);
     const T* F = comp == 0 ? U0 : (comp == 1 ? U1 : U2);
     const T* Qc = comp == 0 ? Q0 : (comp == 1 ? Q1 : Q2);
-    const int ni = g.nx - 2, J = g.ny - 2, nk = g.nz - 2;
-    const long long n = (long long)ni * J * nk;
+    const int J = g.ny - 2, nk = g.nz - 2, nz = g.nz;
+    const int rows = J * nk;
+    const T cE = (T)gc.cE, cW = (T)gc.cW, cN = (T)gc.cN, cS = (T)gc.cS;
     double acc = 0.0;
-    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < n;
-         t0 += (long long)gridDim.x * blockDim.x) {
-        int i = 1 + (int)(t0 % ni);
-        long long r = t0 / ni;
-        int j = 1 + (int)(r % J);
-        int k = 1 + (int)(r / J);
-        long long p = idx(g, i, j, k);
-        const T d = (T)(1.0 + (t * Ap[k]));
-        const T cT = (T)(t * At[k]), cB = (T)(t * Ab[k]);
-        const T cE = (T)gc.cE, cW = (T)gc.cW, cN = (T)gc.cN, cS = (T)gc.cS;
-        T res = Qc[p] - d * F[p] - cE * F[p + 1] - cW * F[p - 1] - cN * F[idx(g, i, jp1(g, j), k)] -
-                cS * F[idx(g, i, jm1(g, j), k)] - cT * F[p + g.ps] - cB * F[p - g.ps];
-        acc += fabs((double)res);
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int j = 1 + r % J, k = 1 + r / J;
+        const T d = (T)pc[4 * nz + k], cT = (T)pc[5 * nz + k], cB = (T)pc[6 * nz + k];
+        const long long row = idx(g, 0, j, k);
+        const long long rjp = idx(g, 0, jp1(g, j), k), rjm = idx(g, 0, jm1(g, j), k);
+        T racc = T(0);
+        for (int i = 1 + threadIdx.x; i <= g.nx - 2; i += blockDim.x) {
+            const long long p = row + i;
+            T res = Qc[p] - d * F[p] - cE * F[p + 1] - cW * F[p - 1] - cN * F[rjp + i] - cS * F[rjm + i] -
+                    cT * F[p + g.ps] - cB * F[p - g.ps];
+            racc += abs(res);
+        }
+        acc += (double)racc;
     }
     double bt = block_sum(acc, s_red);
     grid_finish(bt, rw, comp, gridDim.x, blockIdx.x, &sc->red[comp], 0);
@@ -832,12 +835,10 @@ int launch_gs_resid(tbl_handle* h, const int* comps, int ncomp, int nblocks) {
     int3 cs = make_int3(comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0);
     if (mixed(h))
         k_gs_resid<float><<<dim3(nblocks, ncomp), RED_THREADS, 0, h->stream>>>(
-            g, gc, h->Ab, h->At, h->Ap, t, h->Df[0], h->Df[1], h->Df[2], h->Qf[0], h->Qf[1], h->Qf[2], cs, ncomp,
-            h->red, h->sc);
+            g, gc, h->gs_coef, h->Df[0], h->Df[1], h->Df[2], h->Qf[0], h->Qf[1], h->Qf[2], cs, ncomp, h->red, h->sc);
     else
         k_gs_resid<double><<<dim3(nblocks, ncomp), RED_THREADS, 0, h->stream>>>(
-            g, gc, h->Ab, h->At, h->Ap, t, h->U[0], h->U[1], h->U[2], h->Q[0], h->Q[1], h->Q[2], cs, ncomp, h->red,
-            h->sc);
+            g, gc, h->gs_coef, h->U[0], h->U[1], h->U[2], h->Q[0], h->Q[1], h->Q[2], cs, ncomp, h->red, h->sc);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }

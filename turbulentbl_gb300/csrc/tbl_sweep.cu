@@ -409,9 +409,10 @@ struct Ptr3 {
 };
 
 // Per-plane coefficients of the reassociated GS update (the values the sweep
-// computes per warp): [p0 | p1 | p2 | p3] x nz.
+// computes per warp), [p0 | p1 | p2 | p3] x nz, and of the GS residual
+// (1 + t Ap, t At, t Ab), [d | cT | cB] x nz.
 __global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double* __restrict__ Ap,
-                          const double* __restrict__ At, double* __restrict__ pc) {
+                          const double* __restrict__ At, const double* __restrict__ Ab, double* __restrict__ pc) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nz) return;
     const double rd = 1.0 / (1.0 + (t * Ap[k]));
@@ -419,6 +420,9 @@ __global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double
     pc[nz + k] = -(t * aw_) * rd;
     pc[2 * nz + k] = -(t * as_) * rd;
     pc[3 * nz + k] = -(t * At[k]) * rd;
+    pc[4 * nz + k] = 1.0 + (t * Ap[k]);
+    pc[5 * nz + k] = t * At[k];
+    pc[6 * nz + k] = t * Ab[k];
 }
 
 template <typename T>
@@ -637,7 +641,8 @@ int launch_halo_init(tbl_handle* h, int parity) {
     // per-plane GS coefficients of the operator in use (the adjoint swaps in A^T)
     k_gs_coef<<<(h->g.nz + 127) / 128, 128, 0, h->stream>>>(h->g.nz, -h->cfg.dt / (h->cfg.re),
                                                              1.0 / (h->cfg.dx * h->cfg.dx),
-                                                             1.0 / (h->cfg.dy * h->cfg.dy), h->Ap, h->At, h->gs_coef);
+                                                             1.0 / (h->cfg.dy * h->cfg.dy), h->Ap, h->At, h->Ab,
+                                                             h->gs_coef);
     h->launches++;
     if (h->cfg.precision == TBL_PREC_MIXED)
         k_halo_init<float><<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(

@@ -108,6 +108,7 @@ class RunParams:
     mixed_max_outer: int = 20
     mixed_inner_tol: float = 1.0e-5
     mixed_outer_tol: float = 1.0e-10
+    mixed_true_tol: float = 1.0e-8   # divergence target of the mixed solve (true relative PPE residual)
 
 
 def recycle_plane(nx):
@@ -139,6 +140,7 @@ def make_config(mesh, rp):
     c.errorstop = rp.errorstop
     c.mixed_inner_tol = rp.mixed_inner_tol
     c.mixed_outer_tol = rp.mixed_outer_tol
+    c.mixed_true_tol = rp.mixed_true_tol
     return c
 
 
