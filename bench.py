@@ -170,7 +170,7 @@ def run_cpu(wl, nproc, budget_s, max_steps):
     }
 
 
-def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget):
+def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True):
     import torch
     torch.cuda.set_device(local)
     from turbulentbl_gb300.lib import TblGpu
@@ -212,7 +212,7 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launch_groups": nl[q]} for q in range(ng - 1)}
     out = {"elapsed": elapsed, "host_elapsed": e1 - e0, "recs": recs, "status": st_all, "launches": launches,
            "clocks": clk, "groups": groups}
-    if wl.precision == abi.TBL_PREC_MIXED:
+    if wl.precision == abi.TBL_PREC_MIXED and do_accuracy:
         out["mixed_state"] = g.download(fields=("u", "v", "w", "p"))
         out["mixed_stats"] = g.download_stats()
         out["accuracy_steps"] = warmup + steps
@@ -348,6 +348,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=30.0, help="seconds of CPU time for the CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="mixed workloads: skip the FP64 comparison run")
     ap.add_argument("--adjoint", action="store_true",
                     help="time the discrete adjoint of a window on the 256x96x96 adjoint workload instead")
     ap.add_argument("--window", type=int, default=50)
@@ -399,7 +400,7 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
-                not args.no_cpu, args.cpu_budget)
+                not args.no_cpu, args.cpu_budget, not args.no_accuracy)
     if rank != 0:
         return
     K = args.steps

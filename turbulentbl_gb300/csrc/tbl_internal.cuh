@@ -148,6 +148,7 @@ struct tbl_handle {
     double time;
     bool fluc_updated;
     int coop_ok;
+    int gs_comps_per_launch;       // velocity components one cooperative GS launch can hold (1..3)
     int n_sm;                      // multiprocessors of the device
     // replay
     std::vector<int32_t> replay;

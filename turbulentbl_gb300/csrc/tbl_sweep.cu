@@ -560,8 +560,21 @@ static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T
 }
 
 // GS sweep for the listed components (old-value terms precomputed first);
-// halo buffers ping-pong by `parity`.
+// halo buffers ping-pong by `parity`.  When the components' CTAs cannot all
+// be resident at once, they sweep in consecutive launches.
+static int launch_gs_sweep_chunk(tbl_handle* h, const int* comps, int ncomp, int parity);
+
 int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity) {
+    const int per = h->gs_comps_per_launch > 0 ? h->gs_comps_per_launch : 1;
+    for (int c0 = 0; c0 < ncomp; c0 += per) {
+        const int n = ncomp - c0 < per ? ncomp - c0 : per;
+        const int s = launch_gs_sweep_chunk(h, comps + c0, n, parity);
+        if (s != TBL_OK) return s;
+    }
+    return TBL_OK;
+}
+
+static int launch_gs_sweep_chunk(tbl_handle* h, const int* comps, int ncomp, int parity) {
     if (h->cfg.precision == TBL_PREC_MIXED) {  // delta form: iterate on D with r0 in Qf
         float* F[3] = {h->Df[0], h->Df[1], h->Df[2]};
         const float* Q[3] = {h->Qf[0], h->Qf[1], h->Qf[2]};
@@ -659,9 +672,21 @@ int check_cooperative(tbl_handle* h) {
     TBL_CUDA_TRY(cudaGetDevice(&dev));
     TBL_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     TBL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int per_sm = 0;
-    TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_sweep<SW_GS, double>, KG * 32, 0));
-    h->coop_ok = coop && (long long)per_sm * sms >= 3LL * h->n_cta;
+    // every CTA of a sweep launch must be resident at once (they wait on one
+    // another): the SSOR sweeps need n_cta CTAs, a GS launch n_cta per component
+    const bool mx = h->cfg.precision == TBL_PREC_MIXED;
+    const void* ks[3] = {mx ? (const void*)k_sweep<SW_GS, float> : (const void*)k_sweep<SW_GS, double>,
+                         mx ? (const void*)k_sweep<SW_FWD, float> : (const void*)k_sweep<SW_FWD, double>,
+                         mx ? (const void*)k_sweep<SW_BWD, float> : (const void*)k_sweep<SW_BWD, double>};
+    long long cap[3];
+    for (int q = 0; q < 3; ++q) {
+        int per_sm = 0;
+        TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks[q], KG * 32, 0));
+        cap[q] = (long long)per_sm * sms;
+    }
+    h->coop_ok = coop && cap[0] >= h->n_cta && cap[1] >= h->n_cta && cap[2] >= h->n_cta;
+    h->gs_comps_per_launch = (int)(cap[0] / (h->n_cta > 0 ? h->n_cta : 1));
+    if (h->gs_comps_per_launch > 3) h->gs_comps_per_launch = 3;
     return h->coop_ok ? TBL_OK : TBL_ERR_BAD_ARG;
 }
 
