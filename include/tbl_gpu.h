@@ -54,7 +54,8 @@ extern "C" {
 /* flags */
 #define TBL_FLAG_REPLAY        1  /* follow counts given by tbl_set_replay instead of testing convergence */
 #define TBL_FLAG_PPE_RESIDUAL  2  /* compute the true relative PPE residual after each solve */
-#define TBL_FLAG_DIAGNOSTICS   4  /* divergence / mass-flux / wall-shear / KE diagnostics every step */
+#define TBL_FLAG_DIAGNOSTICS   4  /* accepted for compatibility: the divergence, mass-flux, wall-shear and
+                                     KE diagnostics run every step, as in the reference */
 
 /* Run parameters.  The reference hard-codes all of them as literals
  * (dnstbl2/dnstbl.f90:20-140); here they are one plain struct. */
@@ -139,11 +140,14 @@ typedef struct tbl_stats_out {
     double* uusum; double* vvsum; double* wwsum;
     double* uvsum; double* uwsum; double* vwsum;
     double* deltastar; double* theta; double* ht; double* reth;  /* (nx), last rescaling */
-    double* tauw_sum;                                  /* sumxz(nx) wall-shear accumulator */
-    double* ubulk;                                     /* mass flux at 5 planes (5) */
+    double* tauw_sum;     /* sumxz(nx): span sums of the wall shear, accumulated every step (:1616-1668) */
+    double* ubulk;        /* UbDNS(5): mass flux through the planes i = 5,20,40,60,85 (1-based, clamped
+                             to nx-1), divided by the cross-section area (:1578-1594), last step */
     double lamda03;
     int32_t nstat;
     int32_t pad_;
+    double* tauw_window;  /* sumxz/500 of the last completed 500-step window (:1670-1681); the
+                             reference's Cf is 2 tauw_window / (Ue^2 (ny-2)) */
 } tbl_stats_out;
 
 typedef struct tbl_handle tbl_handle;

@@ -17,6 +17,7 @@ def lib():
         _lib.orc_apply_ssor.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.orc_solve_ppe.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int32)]
+        _lib.orc_flux_shear.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     return _lib
 
 
@@ -43,3 +44,12 @@ class OracleRunner(AbiRunner):
         y = np.zeros_like(x, order="F")
         lib().orc_apply_ssor(self._h, x.ctypes.data_as(C.POINTER(C.c_double)), y.ctypes.data_as(C.POINTER(C.c_double)))
         return y
+
+    def flux_shear(self):
+        """Mass flux at the five planes and per-column span sums of the wall
+        shear of the current state (not accumulated)."""
+        ub = np.zeros(5)
+        tau = np.zeros(self.mesh.nx)
+        lib().orc_flux_shear(self._h, ub.ctypes.data_as(C.POINTER(C.c_double)),
+                             tau.ctypes.data_as(C.POINTER(C.c_double)))
+        return ub, tau

@@ -66,7 +66,7 @@ struct Oracle {
     int nstep = 0, cont = 0, ksep = 0, nstat = 0;
     // statistics
     std::vector<double> usum, vsum, wsum, uusum, vvsum, wwsum, uvsum, uwsum, vwsum;
-    std::vector<double> deltastar, theta, Ht, Reth, sumxz;
+    std::vector<double> deltastar, theta, Ht, Reth, sumxz, tauw_window;
     double ubulk[5] = {0, 0, 0, 0, 0};
     // GMRES work
     std::vector<std::vector<double>> V;
@@ -155,7 +155,7 @@ int setup(Oracle& o, const tbl_config* cfg, const tbl_mesh* m) {
         v->assign(n2, 0.0);
     o.ume1.assign(o.nz, 0.0);
     o.newk.assign(o.nz, o.nz - 1);
-    for (auto* v : {&o.bltkns, &o.deltastar, &o.theta, &o.Ht, &o.Reth, &o.sumxz}) v->assign(o.nx, 0.0);
+    for (auto* v : {&o.bltkns, &o.deltastar, &o.theta, &o.Ht, &o.Reth, &o.sumxz, &o.tauw_window}) v->assign(o.nx, 0.0);
     o.V.assign(cfg->kmax + 1, std::vector<double>(o.N, 0.0));
     o.r.assign(o.N, 0.0); o.rhat.assign(o.N, 0.0);
     int K1 = cfg->kmax + 1;
@@ -716,6 +716,65 @@ double div_diag(const Oracle& o) {
     return std::fabs(tot) / ((double)(ny - 2) * (nx - 2) * (nz - 2));
 }
 
+// Mass flux through five cross-stream planes (:1578-1594): per rank the cell
+// sums over its k range (rank 0 also the first cell layer, the last rank not
+// its top face), ranks summed in order, divided by the area Av (:448).
+// Plane indices are the reference's literals (:95), clamped to nx-1.
+void mass_flux(Oracle& o) {
+    static const int plane[5] = {5, 20, 40, 60, 85};
+    const int nx = o.nx, ny = o.ny, nz = o.nz;
+    const double Av = o.x3[nz - 1] * (o.x2[ny - 2] - o.x2[1]);
+    for (int q = 0; q < 5; ++q) {
+        const int ip = plane[q] < nx - 1 ? plane[q] : nx - 1;
+        double tot = 0.0;
+        for (int rk = 0; rk < o.P; ++rk) {
+            const int k0 = rk == 0 ? o.bn[rk] - 1 : o.bn[rk];
+            double ub = 0.0;
+            for (int k = k0; k <= o.en[rk]; ++k)
+                for (int j = 2; j <= ny - 1; ++j) {
+                    const int jp1 = j == ny - 1 ? 2 : j + 1;
+                    const double dAv = o.dy * (o.x3[k] - o.x3[k - 1]);  // x3(k+1) - x3(k), 1-based
+                    ub = ub + (0.25 * (o.U[0][o.id(ip, j, k)] + o.U[0][o.id(ip, jp1, k)] + o.U[0][o.id(ip, j, k + 1)] +
+                                       o.U[0][o.id(ip, jp1, k + 1)]) * (dAv));
+                }
+            tot += ub;
+        }
+        o.ubulk[q] = tot / Av;
+    }
+}
+
+// Wall shear (:1616-1681): span sum of (dw/dx + du/dz)/Re at the wall per
+// column, accumulated every step in sumxz; every 500 steps the window mean is
+// written (kept here as tauw_window) and the accumulator restarts.
+void wall_shear(Oracle& o, double* tau_out = nullptr) {
+    const int nx = o.nx, ny = o.ny;
+    const double d1 = o.x3[1] - o.x3[0], d2 = o.x3[2] - o.x3[0];
+    const std::vector<double>&U1 = o.U[0], &U3 = o.U[2];
+    for (int i = 2; i <= nx - 1; ++i) {
+        double tauxz = 0.0;
+        for (int j = 2; j <= ny - 1; ++j) {
+            double mfb1;
+            if (i <= 3 || i >= nx - 2)
+                mfb1 = (U3[o.id(i + 1, j, 1)] - U3[o.id(i - 1, j, 1)]) / (2.0 * o.dx);
+            else
+                mfb1 = (-U3[o.id(i - 3, j, 1)] + (9.0 * U3[o.id(i - 2, j, 1)]) - (45.0 * U3[o.id(i - 1, j, 1)]) +
+                        (45.0 * U3[o.id(i + 1, j, 1)]) - (9.0 * U3[o.id(i + 2, j, 1)]) + U3[o.id(i + 3, j, 1)]) /
+                       (60.0 * o.dx);
+            const double fder = (((U1[o.id(i, j, 3)] - U1[o.id(i, j, 1)]) * (d1 * d1)) +
+                                 ((U1[o.id(i, j, 1)] - U1[o.id(i, j, 2)]) * (d2 * d2))) /
+                                ((d2 * (d1 * d1)) - ((d2 * d2) * d1));
+            tauxz = tauxz + ((mfb1 + fder) / o.c.re);
+        }
+        if (tau_out) { tau_out[i - 1] = tauxz; continue; }
+        o.sumxz[i - 1] = tauxz + o.sumxz[i - 1];
+    }
+    if (tau_out) return;
+    if (o.nstep % 500 == 0) {
+        for (int i = 2; i <= nx - 1; ++i) o.tauw_window[i - 1] = o.sumxz[i - 1] / 500.0;
+        for (double& v : o.sumxz) v = 0.0;
+    }
+}
+
 // --------------------------------------------------- a9: statistics per step
 // Ufluc per step (:1707-1722), KE (:1724-1741), stats (:1902-1993)
 void per_step_stats(Oracle& o, double& ke, int& blowup) {
@@ -880,6 +939,8 @@ int one_step(Oracle& o, tbl_step_stats* st) {
     }
     project_bcs(o);
     s.div_diag = div_diag(o);
+    mass_flux(o);
+    wall_shear(o);
     int blow = 0;
     per_step_stats(o, s.ke, blow);
     s.cum_step = 0;
@@ -920,6 +981,9 @@ int orc_create(const tbl_config* cfg, const tbl_mesh* mesh, orc_handle** out) {
 int orc_upload_state(orc_handle* h, const tbl_state* st) {
     if (!h || !st || !st->u || !st->v || !st->w || !st->p) return TBL_ERR_BAD_ARG;
     Oracle& o = h->o;
+    o.sumxz.assign(o.nx, 0.0);
+    o.tauw_window.assign(o.nx, 0.0);
+    for (double& b : o.ubulk) b = 0.0;
     std::memcpy(o.U[0].data(), st->u, o.N * 8);
     std::memcpy(o.U[1].data(), st->v, o.N * 8);
     std::memcpy(o.U[2].data(), st->w, o.N * 8);
@@ -997,6 +1061,21 @@ int orc_download_state(orc_handle* h, tbl_state* st) {
     return TBL_OK;
 }
 
+// Test hook: the mass flux and the per-column span sums of the wall shear of
+// the current state, without accumulating.
+int orc_flux_shear(orc_handle* h, double* ub5, double* tau_nx) {
+    if (!h || !ub5 || !tau_nx) return TBL_ERR_BAD_ARG;
+    Oracle& o = h->o;
+    double keep[5];
+    std::memcpy(keep, o.ubulk, sizeof(keep));
+    mass_flux(o);
+    std::memcpy(ub5, o.ubulk, 5 * 8);
+    std::memcpy(o.ubulk, keep, sizeof(keep));
+    for (int i = 0; i < o.nx; ++i) tau_nx[i] = 0.0;
+    wall_shear(o, tau_nx);
+    return TBL_OK;
+}
+
 int orc_download_stats(orc_handle* h, tbl_stats_out* out) {
     if (!h || !out) return TBL_ERR_BAD_ARG;
     Oracle& o = h->o;
@@ -1010,6 +1089,7 @@ int orc_download_stats(orc_handle* h, tbl_stats_out* out) {
     if (out->reth) std::memcpy(out->reth, o.Reth.data(), o.nx * 8);
     if (out->tauw_sum) std::memcpy(out->tauw_sum, o.sumxz.data(), o.nx * 8);
     if (out->ubulk) std::memcpy(out->ubulk, o.ubulk, 5 * 8);
+    if (out->tauw_window) std::memcpy(out->tauw_window, o.tauw_window.data(), o.nx * 8);
     out->lamda03 = o.lamda03;
     out->nstat = o.nstat;
     return TBL_OK;

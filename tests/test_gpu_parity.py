@@ -78,13 +78,30 @@ def test_statistics_and_rescaling_match():
     a, b = o.download_stats(), g.download_stats()
     for f in ("usum", "vsum", "wsum", "uusum", "vvsum", "wwsum", "uvsum", "uwsum", "vwsum"):
         assert rel(b[f], a[f]) <= 1e-12, f
-    for f in ("deltastar", "theta", "ht", "reth"):
+    for f in ("deltastar", "theta", "ht", "reth", "tauw_sum", "ubulk"):
         assert rel(b[f], a[f]) <= 1e-12, f
+    assert np.abs(a["tauw_sum"]).max() > 0 and np.abs(a["ubulk"]).max() > 0
     assert b["lamda03"] == pytest.approx(a["lamda03"], rel=1e-12)
     sa, sb = o.download(), g.download()
     for f in ("usum2", "vsum2", "wsum2", "wt", "uf", "vf", "wf"):
         assert rel(sb[f], sa[f]) <= 1e-12, f
     assert np.array_equal(sa["newk"], sb["newk"])
+
+
+def test_wall_shear_window_closes_like_the_oracle():
+    """The 500-step wall-shear window (:1670-1681) closes at nstep = 500."""
+    o, g, st = pair(24, 12, 20, 2, cum=10 ** 6)
+    st = dict(st, nstep=497)
+    o.upload(st)
+    g.upload(st)
+    for _ in range(5):
+        o.step(1)
+        g.step(1)
+    a, b = o.download_stats(), g.download_stats()
+    assert np.abs(a["tauw_window"]).max() > 0
+    assert rel(b["tauw_window"], a["tauw_window"]) <= 1e-12
+    assert rel(b["tauw_sum"], a["tauw_sum"]) <= 1e-12  # two steps into the next window
+    assert rel(b["ubulk"], a["ubulk"]) <= 1e-12
 
 
 def test_ppe_residual_reported():

@@ -154,3 +154,34 @@ def test_recycling_map_outer_stretch_is_monotone():
     bl, wt, newk, ksep = rescaling_state(usum2, x3, 1.0, irec=10, lamda=1.05)
     k = newk[:nz - 1]
     assert np.all(np.diff(k) >= 0) and k.min() >= 1 and k.max() <= nz - 1
+
+
+def test_mass_flux_and_wall_shear_known_answers():
+    """Mass flux (:1578-1594) and wall shear (:1616-1668) on fields with known
+    answers.  u = U0 + s x gives, at each plane i_p, (U0 + s x(i_p)) times
+    (ny-2)/(ny-3): the reference divides the flux through the ny-2 unique span
+    cells by an area spanning only x2(ny-1) - x2(2) = (ny-3) dy.  u = a z + e z^2
+    near the wall and w(wall) = b x give the span sum (ny-2)(a + b)/Re in every
+    column (both stencils are exact there)."""
+    wl = small_workload(nx=24, nz_span=10, ny_wall=14)
+    mesh, rp, st = make_state(wl, nproc=2)
+    o = OracleRunner(mesh, rp)
+    X, Y, Z = grids(mesh)
+    assert mesh.x3[0] == 0.0
+    U0, s = 0.7, 0.05
+    st = dict(st, u=np.asfortranarray(U0 + s * X), v=np.zeros_like(X), w=np.zeros_like(X), p=np.zeros_like(X))
+    o.upload(st)
+    ub, _ = o.flux_shear()
+    ratio = (mesh.ny - 2) / (mesh.ny - 3)
+    for q, plane in enumerate((5, 20, 40, 60, 85)):
+        ip = min(plane, mesh.nx - 1) - 1
+        assert ub[q] == pytest.approx((U0 + s * mesh.x1[ip]) * ratio, rel=1e-12)
+    a, e, b = 2.0, -3.0, 0.4
+    w = np.zeros_like(X)
+    w[:, :, 0] = b * X[:, :, 0]
+    st = dict(st, u=np.asfortranarray(a * Z + e * Z * Z), w=np.asfortranarray(w))
+    o.upload(st)
+    _, tau = o.flux_shear()
+    expect = (mesh.ny - 2) * (a + b) / rp.re
+    assert np.allclose(tau[1:-1], expect, rtol=1e-10)
+    assert tau[0] == 0.0 and tau[-1] == 0.0

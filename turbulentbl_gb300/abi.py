@@ -106,6 +106,7 @@ class TblStatsOut(C.Structure):
         ("deltastar", _dp), ("theta", _dp), ("ht", _dp), ("reth", _dp),
         ("tauw_sum", _dp), ("ubulk", _dp),
         ("lamda03", C.c_double), ("nstat", C.c_int32), ("pad_", C.c_int32),
+        ("tauw_window", _dp),
     ]
 
 

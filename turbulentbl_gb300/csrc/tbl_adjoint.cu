@@ -58,6 +58,7 @@ struct AdjTape {
     std::vector<double*> segU1, segU3;  // ck entries of 3 x vol each
     Ckpt fin;
     double* fin_sums = nullptr;
+    double* fin_diag = nullptr;  // sumxz, tauw window, mass flux at the end of the window
     double *lU[3] = {nullptr, nullptr, nullptr}, *lP = nullptr;
     double *lc = nullptr, *AW = nullptr, *LE = nullptr, *luold = nullptr;
     double *ocf = nullptr, *jacc = nullptr;
@@ -831,6 +832,7 @@ int tape_alloc(tbl_handle* h, int W, int ck) {
     const size_t ck_n = 5 * vol + 3 * pl;
     size_t n = (size_t)nseg * ck_n + (size_t)ck * 6 * vol + ck_n + 9 * n2 + 4 * vol;
     n += (size_t)g.nx * (g.ny - 2) + (size_t)g.nx * g.ny + 2 * pl + 4 * (size_t)g.nx + 8;
+    n += 2 * (size_t)g.nx + 8;  // fin_diag
     TBL_CUDA_TRY(cudaMalloc((void**)&T->buf, n * sizeof(double)));
     TBL_CUDA_TRY(cudaMemset(T->buf, 0, n * sizeof(double)));
     T->buf_n = n;
@@ -855,6 +857,7 @@ int tape_alloc(tbl_handle* h, int W, int ck) {
     T->luold = take(pl);
     T->ocf = take(4 * (size_t)g.nx);
     T->jacc = take(8);
+    T->fin_diag = take(2 * (size_t)g.nx + 8);
     T->nstep_of.assign(W, 0);
     return TBL_OK;
 }
@@ -972,6 +975,9 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
     const double J = h->hpin[0] / nsteps;
     ATRY(save_ckpt(h, T->fin));
     ATRY(dcopy(h, T->fin_sums, h->sums, 9 * (size_t)g.nx * g.nz));
+    ATRY(dcopy(h, T->fin_diag, h->sumxz, (size_t)g.nx));
+    ATRY(dcopy(h, T->fin_diag + g.nx, h->tauw_win, (size_t)g.nx));
+    ATRY(dcopy(h, T->fin_diag + 2 * g.nx, h->ubulk, 5));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     T->forward_ms = ms_since(t0);
     if (bm == TBL_BRANCH_RECORD) T->bits_valid = true;
@@ -1042,6 +1048,9 @@ int tbl_backward_window(tbl_handle* h, double dL_dJ, const tbl_fields* dL_dfinal
     // the handle returns to the state at the end of the window
     ATRY(restore_ckpt(h, T->fin));
     ATRY(dcopy(h, h->sums, T->fin_sums, 9 * (size_t)g.nx * g.nz));
+    ATRY(dcopy(h, h->sumxz, T->fin_diag, (size_t)g.nx));
+    ATRY(dcopy(h, h->tauw_win, T->fin_diag + g.nx, (size_t)g.nx));
+    ATRY(dcopy(h, h->ubulk, T->fin_diag + 2 * g.nx, 5));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     if (out) {
         memset(out, 0, sizeof(*out));

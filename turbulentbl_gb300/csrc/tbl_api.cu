@@ -118,7 +118,7 @@ static void free_all(tbl_handle* h) {
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
                     h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->gs_coef, h->usum2, h->vsum2,
                     h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
-                    h->usum2_fl, h->sums, h->bl_out, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
+                    h->usum2_fl, h->sums, h->bl_out, h->ubulk, h->sumxz, h->tauw_win, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
                     h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -191,6 +191,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));
     TRY(dalloc(&h->ufl_full, 3 * vol)); TRY(dalloc(&h->usum2_fl, 3 * n2));
     TRY(dalloc(&h->sums, 9 * n2)); TRY(dalloc(&h->bl_out, 4 * (size_t)nx));
+    TRY(dalloc(&h->ubulk, 5)); TRY(dalloc(&h->sumxz, (size_t)nx)); TRY(dalloc(&h->tauw_win, (size_t)nx));
     TRY(dalloc(&h->slab_of_k, (size_t)nz));
     TRY(dalloc(&h->sc, 1));
     const int K1 = (cfg->precision == TBL_PREC_MIXED ? cfg->mixed_kmax : cfg->kmax) + 1;
@@ -217,6 +218,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     for (int k = 0; k < nz; ++k) jinv[k] = 1.0 / mesh->jac[k];
     h->x3h = x3;
     h->stats_A = mesh->x2[ny - 1] - mesh->x2[1];
+    h->area_mf = x3[nz - 1] * (mesh->x2[ny - 2] - mesh->x2[1]);  // Av (:448)
     TBL_CUDA_TRY(cudaMemcpy(h->x3, x3.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->jacinv, jinv.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->jac2, j2.data(), nz * 8, cudaMemcpyHostToDevice));
@@ -558,6 +560,7 @@ int one_step(tbl_handle* h, tbl_step_stats* out) {
     {
         ProfScope ps_stats(h, TBL_PROF_STATS, (fluc ? 9.0 : 6.0) * wN);
         TRY(launch_div_diag(h, nb > 512 ? 512 : nb, 3));
+        TRY(launch_flux_shear(h));
         if (fluc) {
             TRY(launch_fluc_ke(h, nb > 512 ? 512 : nb, 4));
             const size_t n2 = (size_t)c.nx * c.nz;
@@ -694,6 +697,9 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
     s0.ksep = st->ksep;
     TBL_CUDA_TRY(cudaMemcpy(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemsetAsync(h->sums, 0, 9 * n2 * 8, h->stream));
+    TBL_CUDA_TRY(cudaMemsetAsync(h->ubulk, 0, 5 * 8, h->stream));
+    TBL_CUDA_TRY(cudaMemsetAsync(h->sumxz, 0, (size_t)c.nx * 8, h->stream));
+    TBL_CUDA_TRY(cudaMemsetAsync(h->tauw_win, 0, (size_t)c.nx * 8, h->stream));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->nstep = st->nstep;
     h->cont = st->cont;
@@ -839,11 +845,15 @@ int tbl_download_stats(tbl_handle* h, tbl_stats_out* out) {
     for (int q = 0; q < 4; ++q)
         if (bl[q]) TBL_CUDA_TRY(cudaMemcpyAsync(bl[q], h->bl_out + (size_t)q * c.nx, (size_t)c.nx * 8,
                                                 cudaMemcpyDeviceToHost, h->stream));
+    if (out->tauw_sum)
+        TBL_CUDA_TRY(cudaMemcpyAsync(out->tauw_sum, h->sumxz, (size_t)c.nx * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (out->ubulk) TBL_CUDA_TRY(cudaMemcpyAsync(out->ubulk, h->ubulk, 5 * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (out->tauw_window)
+        TBL_CUDA_TRY(cudaMemcpyAsync(out->tauw_window, h->tauw_win, (size_t)c.nx * 8, cudaMemcpyDeviceToHost,
+                                     h->stream));
     DevScalars sc;
     TBL_CUDA_TRY(cudaMemcpyAsync(&sc, h->sc, sizeof(sc), cudaMemcpyDeviceToHost, h->stream));
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    if (out->tauw_sum) memset(out->tauw_sum, 0, (size_t)c.nx * 8);
-    if (out->ubulk) memset(out->ubulk, 0, 5 * 8);
     out->lamda03 = sc.lamda03;
     out->nstat = h->nstat;
     return TBL_OK;

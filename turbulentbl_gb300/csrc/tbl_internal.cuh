@@ -123,6 +123,10 @@ struct tbl_handle {
     // statistics
     double* sums;      // 9 x (nx,nz): usum vsum wsum uusum vvsum wwsum uvsum uwsum vwsum
     double* bl_out;    // 4 x nx: deltastar theta Ht Reth
+    double* ubulk;     // 5: mass flux through the five planes (last step)
+    double* sumxz;     // nx: wall-shear accumulator
+    double* tauw_win;  // nx: mean of the last completed 500-step window
+    double area_mf;    // Av = x3(nz) (x2(ny-1) - x2(2)) (1-based)
     double stats_A;    // x2(ny) - x2(2) (dnstbl2/dnstbl.f90:442)
     std::vector<double> x3h;  // host copy of x3
     int* slab_of_k;    // nz: slab index of each interior plane

@@ -13,6 +13,7 @@ int launch_div(tbl_handle* h);
 int launch_pc_zero_faces(tbl_handle* h);
 int launch_project_bcs(tbl_handle* h);
 int launch_div_diag(tbl_handle* h, int nblocks, int slot);
+int launch_flux_shear(tbl_handle* h);
 int launch_fluc_ke(tbl_handle* h, int nblocks, int slot);
 int launch_stats(tbl_handle* h);
 int launch_rescale(tbl_handle* h);

@@ -935,6 +935,91 @@ int launch_project_bcs(tbl_handle* h) {
     return TBL_OK;
 }
 
+// ------------------------------------ diagnostics: mass flux, wall shear
+// Mass flux through the five cross-stream planes i = 5, 20, 40, 60, 85
+// (1-based, :95; clamped to nx-1) (:1578-1594): cell averages of u times the
+// cell area dy (x3(k+1) - x3(k)) over the span and the whole height, divided
+// by the area Av.  One block per plane.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mass_flux(Geom g, double dy, double Av, const double* __restrict__ x3,
+                                                   const T* __restrict__ U1, double* __restrict__ ub) {
+    __shared__ double s_red[256 / 32];
+    const int planes[5] = {5, 20, 40, 60, 85};
+    const int q = blockIdx.x;
+    const int ip = (planes[q] < g.nx - 1 ? planes[q] : g.nx - 1) - 1;  // 0-based
+    const int J = g.ny - 2;
+    const int ncell = J * (g.nz - 1);
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+        const int j = 1 + t % J, k = t / J;
+        const int jp = j == g.ny - 2 ? 1 : j + 1;
+        const double dAv = dy * (x3[k + 1] - x3[k]);
+        acc += (0.25 * ((double)U1[idx(g, ip, j, k)] + (double)U1[idx(g, ip, jp, k)] +
+                        (double)U1[idx(g, ip, j, k + 1)] + (double)U1[idx(g, ip, jp, k + 1)]) *
+                (dAv));
+    }
+    acc = block_sum(acc, s_red);
+    if (threadIdx.x == 0) ub[q] = acc / Av;
+}
+
+// Wall shear (:1616-1681): for every interior column the span sum of
+// (dw/dx + du/dz)/Re at the wall -- dw/dx 6th-order central, 2nd order within
+// three points of the ends; du/dz one-sided 2nd order on the stretched grid --
+// added to the accumulator sumxz; at a window end (every 500 steps) the
+// window mean sumxz/500 is kept and the accumulator restarts.  One block per
+// column.
+template <typename T>
+__global__ void __launch_bounds__(128) k_wall_shear(Geom g, double dx, double re, double d1, double d2,
+                                                    const T* __restrict__ U1, const T* __restrict__ U3,
+                                                    double* __restrict__ sumxz, double* __restrict__ window,
+                                                    int close_window) {
+    __shared__ double s_red[128 / 32];
+    const int i = 1 + blockIdx.x;  // 0-based interior column
+    const int nx = g.nx;
+    double acc = 0.0;
+    for (int j = 1 + threadIdx.x; j <= g.ny - 2; j += blockDim.x) {
+        auto w0 = [&](int ii) { return (double)U3[idx(g, ii, j, 0)]; };
+        double mfb1;
+        if (i <= 2 || i >= nx - 3)
+            mfb1 = (w0(i + 1) - w0(i - 1)) / (2.0 * dx);
+        else
+            mfb1 = (-w0(i - 3) + (9.0 * w0(i - 2)) - (45.0 * w0(i - 1)) + (45.0 * w0(i + 1)) - (9.0 * w0(i + 2)) +
+                    w0(i + 3)) /
+                   (60.0 * dx);
+        const double u0 = U1[idx(g, i, j, 0)], u1 = U1[idx(g, i, j, 1)], u2 = U1[idx(g, i, j, 2)];
+        const double fder = (((u2 - u0) * (d1 * d1)) + ((u0 - u1) * (d2 * d2))) / ((d2 * (d1 * d1)) - ((d2 * d2) * d1));
+        acc += ((mfb1 + fder) / re);
+    }
+    acc = block_sum(acc, s_red);
+    if (threadIdx.x == 0) {
+        const double s = acc + sumxz[i];
+        if (close_window) {
+            window[i] = s / 500.0;
+            sumxz[i] = 0.0;
+        } else {
+            sumxz[i] = s;
+        }
+    }
+}
+
+int launch_flux_shear(tbl_handle* h) {
+    const Geom& g = h->g;
+    const double d1 = h->x3h[1] - h->x3h[0], d2 = h->x3h[2] - h->x3h[0];
+    const int close = (h->nstep % 500 == 0) ? 1 : 0;
+    if (close) TBL_CUDA_TRY(cudaMemsetAsync(h->tauw_win, 0, (size_t)g.nx * 8, h->stream));
+    if (mixed(h)) {
+        k_mass_flux<float><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->Uf[0], h->ubulk);
+        k_wall_shear<float><<<g.nx - 2, 128, 0, h->stream>>>(g, h->cfg.dx, h->cfg.re, d1, d2, h->Uf[0], h->Uf[2],
+                                                             h->sumxz, h->tauw_win, close);
+    } else {
+        k_mass_flux<double><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->U[0], h->ubulk);
+        k_wall_shear<double><<<g.nx - 2, 128, 0, h->stream>>>(g, h->cfg.dx, h->cfg.re, d1, d2, h->U[0], h->U[2],
+                                                              h->sumxz, h->tauw_win, close);
+    }
+    h->launches += 2;
+    return TBL_OK;
+}
+
 int launch_div_diag(tbl_handle* h, int nblocks, int slot) {
     const Geom& g = h->g;
     if (mixed(h))

@@ -115,7 +115,7 @@ class AbiRunner:
             a = np.zeros((nx, nz), order="F")
             out[name] = a
             setattr(o, name, abi.dptr(a))
-        for name in ("deltastar", "theta", "ht", "reth", "tauw_sum"):
+        for name in ("deltastar", "theta", "ht", "reth", "tauw_sum", "tauw_window"):
             a = np.zeros(nx)
             out[name] = a
             setattr(o, name, abi.dptr(a))
