@@ -116,7 +116,7 @@ static void free_all(tbl_handle* h) {
     for (void* p : mptrs)
         if (p) cudaFree(p);
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
-                    h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->gs_coef, h->usum2, h->vsum2,
+                    h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->gs_coef, h->gs_coef_f, h->lap_scale, h->coef_f, h->usum2, h->vsum2,
                     h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
                     h->usum2_fl, h->sums, h->bl_out, h->ubulk, h->sumxz, h->tauw_win, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
                     h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
@@ -186,6 +186,9 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
     TRY(dalloc(&h->rAp, (size_t)nz));
     TRY(dalloc(&h->gs_coef, 7 * (size_t)nz));
+    TRY(dalloc(&h->gs_coef_f, 4 * (size_t)nz));
+    TRY(dalloc(&h->lap_scale, (size_t)nz));
+    TRY(dalloc(&h->coef_f, 4 * (size_t)nz));
     TRY(dalloc(&h->usum2, n2)); TRY(dalloc(&h->vsum2, n2)); TRY(dalloc(&h->wsum2, n2)); TRY(dalloc(&h->wt, n2));
     TRY(dalloc(&h->ume1, (size_t)nz)); TRY(dalloc(&h->bltkns, (size_t)nx)); TRY(dalloc(&h->newk, (size_t)nz));
     TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));
@@ -226,6 +229,17 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TBL_CUDA_TRY(cudaMemcpy(h->At, At.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->Ap, Ap.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->rAp, rAp.data(), nz * 8, cudaMemcpyHostToDevice));
+    {   // the forward sweep's -w/Ap(k) in FP64, and the FP32 matvec's coefficients (casts of the FP64 values)
+        std::vector<double> sc(nz, 0.0);
+        std::vector<float> cf(4 * (size_t)nz, 0.0f);
+        for (int k = 0; k < nz; ++k) {
+            sc[k] = -cfg->omega * rAp[k];
+            cf[k] = (float)Ab[k]; cf[nz + k] = (float)At[k]; cf[2 * nz + k] = (float)Ap[k];
+            cf[3 * nz + k] = (float)sc[k];
+        }
+        TBL_CUDA_TRY(cudaMemcpy(h->lap_scale, sc.data(), nz * 8, cudaMemcpyHostToDevice));
+        TBL_CUDA_TRY(cudaMemcpy(h->coef_f, cf.data(), 4 * (size_t)nz * 4, cudaMemcpyHostToDevice));
+    }
     std::vector<double> AbT(nz, 0.0), AtT(nz, 0.0);  // L7^T: row k couples k-1 by At[k-1], k+1 by Ab[k+1]
     for (int k = 1; k <= nz - 2; ++k) { AbT[k] = At[k - 1]; AtT[k] = Ab[k + 1]; }
     TRY(dalloc(&h->AbT, (size_t)nz)); TRY(dalloc(&h->AtT, (size_t)nz));

@@ -98,6 +98,9 @@ struct tbl_handle {
     double* PRE;     // 3 x vol: old-value terms of the GS point updates (FP64)
     float* PREf;     // 3 x vol: the same in mixed precision
     double* gs_coef; // 7 x nz per-plane coefficients of the GS update and residual
+    float* gs_coef_f;   // 4 x nz: the update coefficients rounded to FP32
+    double* lap_scale;  // nz: -w/Ap(k), the SSOR forward scaling folded into the matvec
+    float* coef_f;      // 4 x nz FP32: Ab, At, Ap, -w/Ap (FP32 matvec)
     double* V;       // kmax+1 Krylov vectors, vol each
     double* uold1;   // U1 at i=1 before the inflow update, (ny, nz)
     // mixed precision (TBL_PREC_MIXED): FP32 fields and inner-GMRES vectors

@@ -315,51 +315,40 @@ __device__ __forceinline__ float dot4f(float4 a, float4 b) {
     return fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
 }
 
-// d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the group's i; per-thread FP32
-// partials over up to 4 float4 (16 products) are accumulated in FP64, blocks
-// reduce in FP64 and the last block of each group sums the partials in block
-// order (deterministic).
+// d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the G basis vectors of group
+// blockIdx.y (first vector g0 + G*blockIdx.y).  Each thread sums its FP32
+// products over its share of the points (a few float4 at most) and converts
+// once; blocks reduce in FP64 and the last block of each group sums the
+// partials in block order (deterministic).
+template <int G>
 __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
                                                             const float4* __restrict__ V, long long vstride4, int nv,
-                                                            double* __restrict__ partial, unsigned int* __restrict__ count,
-                                                            int max_blocks, double* __restrict__ dout,
-                                                            double* __restrict__ gout) {
+                                                            int g0, double* __restrict__ partial,
+                                                            unsigned int* __restrict__ count, int max_blocks,
+                                                            double* __restrict__ dout, double* __restrict__ gout) {
     __shared__ double s_red[RED_THREADS / 32];
     __shared__ bool s_last;
-    const int i0 = blockIdx.y * LSG_G;
-    const int ng = min(LSG_G, nv - i0);
+    const int grp = g0 / LSG_G + blockIdx.y;  // slot index of this group
+    const int i0 = g0 + blockIdx.y * G;
     const float4* vl = V + (long long)(nv - 1) * vstride4;
-    double ad[LSG_G], ag[LSG_G];
+    float fd[G], fg[G];
 #pragma unroll
-    for (int e = 0; e < LSG_G; ++e) { ad[e] = 0.0; ag[e] = 0.0; }
+    for (int e = 0; e < G; ++e) { fd[e] = 0.f; fg[e] = 0.f; }
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; q0 < n4; q0 += 4 * stride) {
-        float fd[LSG_G], fg[LSG_G];
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
+        const float4 x = w[q], l = vl[q];
 #pragma unroll
-        for (int e = 0; e < LSG_G; ++e) { fd[e] = 0.f; fg[e] = 0.f; }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const long long q = q0 + u * stride;
-            if (q < n4) {
-                const float4 x = w[q], l = vl[q];
-#pragma unroll
-                for (int e = 0; e < LSG_G; ++e)
-                    if (e < ng) {
-                        const float4 v = V[(long long)(i0 + e) * vstride4 + q];
-                        fd[e] += dot4f(v, x);
-                        fg[e] += dot4f(v, l);
-                    }
-            }
+        for (int e = 0; e < G; ++e) {
+            const float4 v = V[(long long)(i0 + e) * vstride4 + q];
+            fd[e] += dot4f(v, x);
+            fg[e] += dot4f(v, l);
         }
-#pragma unroll
-        for (int e = 0; e < LSG_G; ++e) { ad[e] += (double)fd[e]; ag[e] += (double)fg[e]; }
     }
-    const size_t base = (size_t)blockIdx.y * 2 * LSG_G;
+    const size_t base = (size_t)grp * 2 * LSG_G;
 #pragma unroll
-    for (int e = 0; e < LSG_G; ++e) {
-        if (e >= ng) break;
-        const double bd = block_sum(ad[e], s_red);
-        const double bg = block_sum(ag[e], s_red);
+    for (int e = 0; e < G; ++e) {
+        const double bd = block_sum((double)fd[e], s_red);
+        const double bg = block_sum((double)fg[e], s_red);
         if (threadIdx.x == 0) {
             partial[(base + 2 * e) * max_blocks + blockIdx.x] = bd;
             partial[(base + 2 * e + 1) * max_blocks + blockIdx.x] = bg;
@@ -367,12 +356,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
     }
     if (threadIdx.x == 0) {
         __threadfence();
-        s_last = atomicAdd(&count[blockIdx.y], 1u) == gridDim.x - 1;
+        s_last = atomicAdd(&count[grp], 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    for (int v = 0; v < 2 * ng; ++v) {
+    for (int v = 0; v < 2 * G; ++v) {
         double acc = 0.0;
         for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&partial[(base + v) * max_blocks + b]);
         acc = block_sum(acc, s_red);
@@ -382,7 +371,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
             else if (i < nv - 1) gout[i] = acc;
         }
     }
-    if (threadIdx.x == 0) count[blockIdx.y] = 0u;
+    if (threadIdx.x == 0) count[grp] = 0u;
 }
 
 // New row of L (row nv-1: <v_{nv-1}, v_j>, j < nv-1), then (I + L) t = d by
@@ -442,21 +431,37 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
     if (kit > 64 || kit > K1) return TBL_ERR_BAD_ARG;
     const int nb = red_blocks(h);
     const long long n4 = h->g.vol / 4;
-    // dot pass: the groups together fill one resident wave (3 blocks of 256 per SM at its register use)
-    const int ngr = (kit + LSG_G - 1) / LSG_G;
-    int nbd = (3 * (h->n_sm > 0 ? h->n_sm : 148)) / ngr;
+    // dot pass: full groups of 8 vectors, then the remainder group; about 16
+    // float4 per thread
+    int nbd = (int)((n4 + RED_THREADS * 16 - 1) / (RED_THREADS * 16));
     if (nbd < 1) nbd = 1;
     if (nbd > nb) nbd = nb;
-    dim3 grid(nbd, ngr);
-    k_lsg_dots_f<<<grid, RED_THREADS, 0, h->stream>>>(n4, (const float4*)W, (const float4*)h->Vf, n4, kit,
-                                                      h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d,
-                                                      h->lsg_g);
+    const int nfull = kit / LSG_G, rem = kit % LSG_G;
+    const float4* Wc = (const float4*)W;
+    const float4* Vc = (const float4*)h->Vf;
+    if (nfull > 0)
+        k_lsg_dots_f<LSG_G><<<dim3(nbd, nfull), RED_THREADS, 0, h->stream>>>(
+            n4, Wc, Vc, n4, kit, 0, h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d, h->lsg_g);
+    if (rem > 0) {
+        const int g0 = nfull * LSG_G;
+        switch (rem) {
+#define TBL_LSG_REM(R)                                                                                              \
+    case R:                                                                                                         \
+        k_lsg_dots_f<R><<<dim3(nbd, 1), RED_THREADS, 0, h->stream>>>(n4, Wc, Vc, n4, kit, g0, h->lsg_partial,       \
+                                                                    h->lsg_count, h->red.max_blocks, h->lsg_d,     \
+                                                                    h->lsg_g);                                      \
+        break;
+            TBL_LSG_REM(1) TBL_LSG_REM(2) TBL_LSG_REM(3) TBL_LSG_REM(4) TBL_LSG_REM(5) TBL_LSG_REM(6)
+            TBL_LSG_REM(7)
+#undef TBL_LSG_REM
+        }
+    }
     k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);  // kit <= 63
     int nbu = 6 * (h->n_sm > 0 ? h->n_sm : 148);  // one resident wave at 6 blocks per SM
     if (nbu > nb) nbu = nb;
     k_lsg_update_f<<<nbu, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
                                                       &hcol[kit]);
-    h->launches += 3;
+    h->launches += 2 + (nfull > 0) + (rem > 0);
     return TBL_OK;
 }
 

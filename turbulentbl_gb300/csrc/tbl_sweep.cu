@@ -412,7 +412,8 @@ struct Ptr3 {
 // computes per warp), [p0 | p1 | p2 | p3] x nz, and of the GS residual
 // (1 + t Ap, t At, t Ab), [d | cT | cB] x nz.
 __global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double* __restrict__ Ap,
-                          const double* __restrict__ At, const double* __restrict__ Ab, double* __restrict__ pc) {
+                          const double* __restrict__ At, const double* __restrict__ Ab, double* __restrict__ pc,
+                          float* __restrict__ pcf) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nz) return;
     const double rd = 1.0 / (1.0 + (t * Ap[k]));
@@ -423,10 +424,11 @@ __global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double
     pc[4 * nz + k] = 1.0 + (t * Ap[k]);
     pc[5 * nz + k] = t * At[k];
     pc[6 * nz + k] = t * Ab[k];
+    for (int q = 0; q < 4; ++q) pcf[q * nz + k] = (float)pc[q * nz + k];  // the FP32 sweep's (float) casts
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_gs_pre(Geom g, const double* __restrict__ pc,
+__global__ void __launch_bounds__(256) k_gs_pre(Geom g, const T* __restrict__ pc,
                                                 const int* __restrict__ slab_of_k,
                                                 const SlabDesc* __restrict__ slabs, int P, int c0_, int c1_, int c2_,
                                                 Ptr3<T> Fs, Ptr3<T> Qs, Ptr3<T> PREs,
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const double* __restrict
     const T* F = Fs.p[comp];
     const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
     const int nz = g.nz;
-    const T p0 = (T)pc[k], p1 = (T)pc[nz + k], p2 = (T)pc[2 * nz + k], p3 = (T)pc[3 * nz + k];
+    const T p0 = pc[k], p1 = pc[nz + k], p2 = pc[2 * nz + k], p3 = pc[3 * nz + k];
     const int jp = (j == g.ny - 2) ? 1 : j + 1;
     const int r = slab_of_k[k];
     const SlabDesc sl = slabs[r];
@@ -457,11 +459,13 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const double* __restrict
 // With rAp non-null the result is multiplied by the forward sweep's
 // coefficient -w/Ap(k) (rounded to the sweep's type first, as the sweep did).
 template <typename TI, typename TO, typename TC>
-__global__ void __launch_bounds__(256) k_lap(Geom g, double aw_, double as_, const double* __restrict__ Ab,
-                                             const double* __restrict__ At, const double* __restrict__ Ap,
+// Coefficient tables come in the arithmetic type TC (and the scale in the
+// output type TO), so an FP32 matvec does no double-to-float conversion per
+// point (those run at the FP64 rate).
+__global__ void __launch_bounds__(256) k_lap(Geom g, TC aw, TC as, const TC* __restrict__ Ab,
+                                             const TC* __restrict__ At, const TC* __restrict__ Ap,
                                              const TI* __restrict__ X, const double* __restrict__ Q8,
-                                             TO* __restrict__ R, double omega, const double* __restrict__ rAp) {
-    const TC aw = (TC)aw_, as = (TC)as_;
+                                             TO* __restrict__ R, const TO* __restrict__ scale) {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
@@ -469,10 +473,10 @@ __global__ void __launch_bounds__(256) k_lap(Geom g, double aw_, double as_, con
     const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
     const TC xjm = (TC)X[(long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k)];
     const TC xjp = (TC)X[(long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k)];
-    TC lap = aw * (TC)X[p - 1] + aw * (TC)X[p + 1] + as * xjm + as * xjp + (TC)Ab[k] * (TC)X[p - g.ps] +
-             (TC)At[k] * (TC)X[p + g.ps] + (TC)Ap[k] * (TC)X[p];
+    TC lap = aw * (TC)X[p - 1] + aw * (TC)X[p + 1] + as * xjm + as * xjp + Ab[k] * (TC)X[p - g.ps] +
+             At[k] * (TC)X[p + g.ps] + Ap[k] * (TC)X[p];
     const TO r = (TO)(Q8 ? ((TC)Q8[p] - (lap)) : lap);
-    R[p] = rAp ? (TO)(-omega * rAp[k]) * r : r;
+    R[p] = scale ? scale[k] * r : r;
 }
 
 // ------------------------------------------------------------- host glue
@@ -552,7 +556,8 @@ static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T
     Ptr3<T> Fs, Qs, Ps;
     for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; Ps.p[c] = PRE[c]; }
     dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
-    k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, h->gs_coef, h->slab_of_k, h->slabs, h->P,
+    const T* pc = sizeof(T) == 8 ? (const T*)h->gs_coef : (const T*)h->gs_coef_f;
+    k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, pc, h->slab_of_k, h->slabs, h->P,
                                              comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0, Fs, Qs,
                                              Ps, a.halo_in);
     h->launches++;
@@ -592,7 +597,7 @@ int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
     const Geom& g = h->g;
     k_lap<double, double, double><<<dim3((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2), 256, 0, h->stream>>>(
         g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
-        h->cfg.omega, h->rAp);
+        h->lap_scale);
     h->launches++;
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
@@ -614,10 +619,11 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
     const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
     if (PCd)
         k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf,
-                                                                  h->cfg.omega, h->rAp);
+                                                                  h->coef_f + 3 * (size_t)g.nz);
     else
-        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, Xf, nullptr, h->RHf,
-                                                                h->cfg.omega, h->rAp);
+        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, (float)aw, (float)as, h->coef_f,
+                                                                h->coef_f + g.nz, h->coef_f + 2 * (size_t)g.nz, Xf,
+                                                                nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz);
     h->launches++;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
@@ -655,7 +661,7 @@ int launch_halo_init(tbl_handle* h, int parity) {
     k_gs_coef<<<(h->g.nz + 127) / 128, 128, 0, h->stream>>>(h->g.nz, -h->cfg.dt / (h->cfg.re),
                                                              1.0 / (h->cfg.dx * h->cfg.dx),
                                                              1.0 / (h->cfg.dy * h->cfg.dy), h->Ap, h->At, h->Ab,
-                                                             h->gs_coef);
+                                                             h->gs_coef, h->gs_coef_f);
     h->launches++;
     if (h->cfg.precision == TBL_PREC_MIXED)
         k_halo_init<float><<<dim3(32, 3 * 2 * h->P), 256, 0, h->stream>>>(
