@@ -411,7 +411,8 @@ def main():
     tg = groups[top]
     launches_top = tg["launch_groups"]
     achieved = tg["bytes"] / (tg["ms"] * 1e-3) / 1e9 if tg["ms"] > 0 else 0.0
-    tt = traffic_table().get(top)
+    tab = traffic_table()
+    tt = tab.get(f"{wl.name}/{top}", tab.get(top))
     traffic = tt.get("bytes_per_launch") if isinstance(tt, dict) else tt
     roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
