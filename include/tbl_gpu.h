@@ -54,6 +54,10 @@ extern "C" {
 /* flags */
 #define TBL_FLAG_REPLAY        1  /* follow counts given by tbl_set_replay instead of testing convergence */
 #define TBL_FLAG_PPE_RESIDUAL  2  /* compute the true relative PPE residual after each solve */
+#define TBL_FLAG_RB_ORDER      8  /* throughput mode, not the reference's arithmetic: red-black (i+j+k odd/even)
+                                     ordering of the implicit-diffusion Gauss-Seidel sweeps and of the SSOR
+                                     preconditioner (one global block, periodic in j), so every sweep is two
+                                     fully parallel passes; the converged solves are the same */
 #define TBL_FLAG_DIAGNOSTICS   4  /* accepted for compatibility: the divergence, mass-flux, wall-shear and
                                      KE diagnostics run every step, as in the reference */
 

@@ -185,8 +185,8 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->x3, (size_t)nz)); TRY(dalloc(&h->jacinv, (size_t)nz)); TRY(dalloc(&h->jac2, (size_t)nz));
     TRY(dalloc(&h->Ab, (size_t)nz)); TRY(dalloc(&h->At, (size_t)nz)); TRY(dalloc(&h->Ap, (size_t)nz));
     TRY(dalloc(&h->rAp, (size_t)nz));
-    TRY(dalloc(&h->gs_coef, 7 * (size_t)nz));
-    TRY(dalloc(&h->gs_coef_f, 4 * (size_t)nz));
+    TRY(dalloc(&h->gs_coef, 8 * (size_t)nz));
+    TRY(dalloc(&h->gs_coef_f, 5 * (size_t)nz));
     TRY(dalloc(&h->lap_scale, (size_t)nz));
     TRY(dalloc(&h->coef_f, 4 * (size_t)nz));
     TRY(dalloc(&h->usum2, n2)); TRY(dalloc(&h->vsum2, n2)); TRY(dalloc(&h->wsum2, n2)); TRY(dalloc(&h->wt, n2));
@@ -640,6 +640,7 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
         (cfg->mixed_kmax < 1 || cfg->mixed_kmax > 63 || cfg->mixed_max_outer < 1 || !(cfg->mixed_true_tol >= 0) || !(cfg->mixed_outer_tol > 0) || !(cfg->mixed_inner_tol > 0)))
         return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED && (cfg->flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
+    if ((cfg->flags & TBL_FLAG_RB_ORDER) && ((cfg->ny - 2) % 2 != 0)) return TBL_ERR_BAD_ARG;  // colouring vs wrap
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TBL_ERR_NO_DEVICE;
     tbl_handle* h = new (std::nothrow) tbl_handle();

@@ -97,8 +97,8 @@ struct tbl_handle {
     double* RH;      // SSOR forward result (scaled)
     double* PRE;     // 3 x vol: old-value terms of the GS point updates (FP64)
     float* PREf;     // 3 x vol: the same in mixed precision
-    double* gs_coef; // 7 x nz per-plane coefficients of the GS update and residual
-    float* gs_coef_f;   // 4 x nz: the update coefficients rounded to FP32
+    double* gs_coef; // 8 x nz per-plane coefficients of the GS update, residual and red-black update
+    float* gs_coef_f;   // 5 x nz: the update coefficients rounded to FP32 (+ the red-black U(k-1) one)
     double* lap_scale;  // nz: -w/Ap(k), the SSOR forward scaling folded into the matvec
     float* coef_f;      // 4 x nz FP32: Ab, At, Ap, -w/Ap (FP32 matvec)
     double* V;       // kmax+1 Krylov vectors, vol each

@@ -424,7 +424,9 @@ __global__ void k_gs_coef(int nz, double t, double aw_, double as_, const double
     pc[4 * nz + k] = 1.0 + (t * Ap[k]);
     pc[5 * nz + k] = t * At[k];
     pc[6 * nz + k] = t * Ab[k];
+    pc[7 * nz + k] = -(t * Ab[k]) * rd;  // red-black GS: coefficient of U(k-1)
     for (int q = 0; q < 4; ++q) pcf[q * nz + k] = (float)pc[q * nz + k];  // the FP32 sweep's (float) casts
+    pcf[4 * nz + k] = (float)pc[7 * nz + k];
 }
 
 template <typename T>
@@ -452,6 +454,60 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const T* __restrict__ pc
     T x = fma(p1, F[line + i + 1], p0 * Qs.p[comp][line + i]);
     if (jp != 1) x = fma(p2, F[(long long)g.sx * ((long long)jp + (long long)g.ny * k) + i], x);
     const_cast<T*>(PREs.p[comp])[line + i] = fma(p3, Fkp[i], x);
+}
+
+// ------------------------------ red-black ordering (TBL_FLAG_RB_ORDER)
+// Throughput mode, not the reference's arithmetic.  Points are coloured by
+// the parity of i+j+k (the number of unique span rows is even, so the
+// periodic wrap keeps the colouring); every neighbour of a point has the other
+// colour, so a colour pass updates all its points at once.
+
+// Gauss-Seidel half sweep of the listed components over one colour, the whole
+// domain as one block (no slab halos), periodic in j:
+//   U = p0 Q + p1 (U(i+1) + U(i-1)) + p2 (U(j+1) + U(j-1)) + p3 U(k+1) + pb U(k-1)
+// with the per-plane coefficients of the GS update (k_gs_coef).
+template <typename T>
+__global__ void __launch_bounds__(256) k_rb_gs(Geom g, const T* __restrict__ pc, const T* __restrict__ pbv,
+                                               Ptr3<T> Fs, Ptr3<T> Qs, int c0_, int c1_, int c2_, int color) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y;
+    const int K = g.nz - 2;
+    const int ci = blockIdx.z / K, k = 1 + blockIdx.z % K;
+    if (i > g.nx - 2 || ((i + j + k) & 1) != color) return;
+    const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
+    T* F = const_cast<T*>(Fs.p[comp]);
+    const int nz = g.nz;
+    const T p0 = pc[k], p1 = pc[nz + k], p2 = pc[2 * nz + k], p3 = pc[3 * nz + k], pb = pbv[k];
+    const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
+    const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
+    const long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
+    const long long pjp = (long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k);
+    F[p] = p0 * Qs.p[comp][p] + p1 * (F[p + 1] + F[p - 1]) + p2 * (F[pjp] + F[pjm]) + p3 * F[p + g.ps] +
+           pb * F[p - g.ps];
+}
+
+// Red-black SSOR preconditioner (one global block, periodic in j), the same
+// splitting and sign convention as the lexicographic one: with RH = -w r/Ap
+// from the matvec and c = -w (2-w)/w,
+//   pass 1, black (odd) points: OUT = c (RH + s_k N(RH))
+//   pass 2, red (even) points:  OUT = c RH + s_k N(OUT)
+// where N(X) = Aw (X(i+1)+X(i-1)) + As (X(j+1)+X(j-1)) + Ab X(k-1) + At X(k+1)
+// and s_k = -w/Ap(k).  Faces of RH and OUT are zero.
+template <typename T>
+__global__ void __launch_bounds__(256) k_rb_ssor(Geom g, T aw, T as, const T* __restrict__ Ab,
+                                                 const T* __restrict__ At, const T* __restrict__ sk, T cfac,
+                                                 const T* __restrict__ RH, T* __restrict__ OUT, int pass) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    const int color = pass == 1 ? 1 : 0;
+    if (i > g.nx - 2 || ((i + j + k) & 1) != color) return;
+    const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
+    const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
+    const long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
+    const long long pjp = (long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k);
+    const T* X = pass == 1 ? RH : OUT;
+    const T nb = aw * (X[p + 1] + X[p - 1]) + as * (X[pjp] + X[pjm]) + Ab[k] * X[p - g.ps] + At[k] * X[p + g.ps];
+    OUT[p] = pass == 1 ? cfac * (RH[p] + sk[k] * nb) : cfac * RH[p] + sk[k] * nb;
 }
 
 // r = L7 X (Q8 == nullptr) or r = Q8 - L7 X on the interior, written to R
@@ -569,7 +625,32 @@ static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T
 // be resident at once, they sweep in consecutive launches.
 static int launch_gs_sweep_chunk(tbl_handle* h, const int* comps, int ncomp, int parity);
 
+template <typename T>
+static int rb_gs(tbl_handle* h, T* const F[3], const T* const Q[3], const T* pc, const T* pb, const int* comps,
+                 int ncomp) {
+    const Geom& g = h->g;
+    Ptr3<T> Fs, Qs;
+    for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; }
+    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
+    for (int color = 0; color < 2; ++color)
+        k_rb_gs<T><<<grid, 256, 0, h->stream>>>(g, pc, pb, Fs, Qs, comps[0], ncomp > 1 ? comps[1] : 0,
+                                                ncomp > 2 ? comps[2] : 0, color);
+    h->launches += 2;
+    return TBL_OK;
+}
+
 int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity) {
+    if (h->cfg.flags & TBL_FLAG_RB_ORDER) {
+        const int nz = h->g.nz;
+        if (h->cfg.precision == TBL_PREC_MIXED) {
+            float* F[3] = {h->Df[0], h->Df[1], h->Df[2]};
+            const float* Q[3] = {h->Qf[0], h->Qf[1], h->Qf[2]};
+            return rb_gs<float>(h, F, Q, h->gs_coef_f, h->gs_coef_f + 4 * (size_t)nz, comps, ncomp);
+        }
+        double* F[3] = {h->U[0], h->U[1], h->U[2]};
+        const double* Q[3] = {h->Q[0], h->Q[1], h->Q[2]};
+        return rb_gs<double>(h, F, Q, h->gs_coef, h->gs_coef + 7 * (size_t)nz, comps, ncomp);
+    }
     const int per = h->gs_comps_per_launch > 0 ? h->gs_comps_per_launch : 1;
     for (int c0 = 0; c0 < ncomp; c0 += per) {
         const int n = ncomp - c0 < per ? ncomp - c0 : per;
@@ -599,12 +680,28 @@ int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
         g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
         h->lap_scale);
     h->launches++;
+    if (h->cfg.flags & TBL_FLAG_RB_ORDER) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     return launch_sweep<SW_FWD, double>(h, a, 1);
 }
 
+template <typename T>
+static int rb_ssor(tbl_handle* h, T aw, T as, const T* Ab, const T* At, const T* sk, const T* RH, T* out) {
+    const Geom& g = h->g;
+    const double w = h->cfg.omega;
+    const T cfac = (T)(-w * ((2.0 - w) / w));
+    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
+    k_rb_ssor<T><<<grid, 256, 0, h->stream>>>(g, aw, as, Ab, At, sk, cfac, RH, out, 1);
+    k_rb_ssor<T><<<grid, 256, 0, h->stream>>>(g, aw, as, Ab, At, sk, cfac, RH, out, 2);
+    h->launches += 2;
+    return TBL_OK;
+}
+
 int launch_ssor_bwd(tbl_handle* h, double* out) {
+    if (h->cfg.flags & TBL_FLAG_RB_ORDER)
+        return rb_ssor<double>(h, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At,
+                               h->lap_scale, h->RH, out);
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     a.OUT = out;
@@ -625,12 +722,18 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
                                                                 h->coef_f + g.nz, h->coef_f + 2 * (size_t)g.nz, Xf,
                                                                 nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz);
     h->launches++;
+    if (h->cfg.flags & TBL_FLAG_RB_ORDER) return TBL_OK;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
     return launch_sweep<SW_FWD, float>(h, a, 1);
 }
 
 int launch_ssor_bwd_f(tbl_handle* h, float* out) {
+    if (h->cfg.flags & TBL_FLAG_RB_ORDER) {
+        const size_t nz = (size_t)h->g.nz;
+        return rb_ssor<float>(h, (float)(1.0 / (h->cfg.dx * h->cfg.dx)), (float)(1.0 / (h->cfg.dy * h->cfg.dy)),
+                              h->coef_f, h->coef_f + nz, h->coef_f + 3 * nz, h->RHf, out);
+    }
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
     a.OUT = out;
