@@ -21,10 +21,14 @@ def rel(a, b):
 
 
 def _pair(precision):
+    """FP64: tight tolerances on both sides.  Mixed: the settings of the
+    mixed-precision tests (an FP32 Gauss-Seidel cannot reach 1e-12)."""
     from turbulentbl_gb300.lib import TblGpu
-    wl = small_workload(nx=24, nz_span=12, ny_wall=20, kmax=20, errtol=1e-12)
+    fp64 = precision == abi.TBL_PREC_FP64
+    wl = small_workload(nx=24, nz_span=12, ny_wall=20, kmax=20, errtol=1e-12 if fp64 else 1e-10)
     mesh, rp, st = make_state(wl, nproc=2)
-    rp.errorstop = 1e-12
+    if fp64:
+        rp.errorstop = 1e-12
     rp.mmax = 3000
     o = OracleRunner(mesh, rp)
     o.upload(st)
@@ -32,7 +36,7 @@ def _pair(precision):
     if precision == abi.TBL_PREC_MIXED:
         rp.precision = abi.TBL_PREC_MIXED
         rp.mixed_kmax = 20
-        rp.mixed_outer_tol = 1e-12
+        rp.mixed_outer_tol = 1e-10
         rp.mixed_inner_tol = 1e-5
     g = TblGpu(mesh, rp)
     g.upload(st)
