@@ -170,7 +170,9 @@ def run_cpu(wl, nproc, budget_s, max_steps):
     }
 
 
-def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True, rb=False):
+def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True, rb=0):
+    """rb: 0 reference ordering, 1 red-black diffusion sweeps, 2 red-black
+    diffusion sweeps and SSOR preconditioner."""
     import torch
     torch.cuda.set_device(local)
     from turbulentbl_gb300.lib import TblGpu
@@ -179,6 +181,8 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
         rp.flags |= abi.TBL_FLAG_PPE_RESIDUAL  # the true ||L7 p' - Q8|| / ||Q8|| every step (one extra pass)
     if rb:
         rp.flags |= abi.TBL_FLAG_RB_ORDER
+    if rb > 1:
+        rp.flags |= abi.TBL_FLAG_RB_PRECOND
     g = TblGpu(mesh, rp)
     g.upload(st)
     for _ in range(warmup):
@@ -353,7 +357,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="mixed workloads: skip the FP64 comparison run")
     ap.add_argument("--rb", action="store_true",
-                    help="red-black throughput mode (TBL_FLAG_RB_ORDER): not the reference's sweep order")
+                    help="red-black diffusion sweeps (TBL_FLAG_RB_ORDER): not the reference's sweep order")
+    ap.add_argument("--rb-precond", action="store_true",
+                    help="with --rb, the SSOR preconditioner red-black ordered too (TBL_FLAG_RB_PRECOND)")
     ap.add_argument("--adjoint", action="store_true",
                     help="time the discrete adjoint of a window on the 256x96x96 adjoint workload instead")
     ap.add_argument("--window", type=int, default=50)
@@ -388,8 +394,11 @@ def main():
               "gmres_tol": wl.errtol, "re_theta": wl.re_theta, "cfl": wl.cfl, "seed": wl.seed,
               "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
               "l2": "inputs larger than L2 (fields 68 MB+, Krylov basis 2.8 GB)",
-              "ordering": ("red-black (throughput mode, not the reference's sweep order)" if args.rb
-                           else "reference (lexicographic block Gauss-Seidel / block SSOR)")}
+              "ordering": ("red-black Gauss-Seidel and SSOR (throughput mode, not the reference's sweep order)"
+                           if args.rb and args.rb_precond else
+                           "red-black Gauss-Seidel, reference block SSOR (throughput mode, not the reference's "
+                           "sweep order)" if args.rb else
+                           "reference (lexicographic block Gauss-Seidel / block SSOR)")}
     metric = "Mpt-steps/s"
     if args.impl == "reference":
         if rank != 0:
@@ -407,7 +416,7 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
-                not args.no_cpu, args.cpu_budget, not args.no_accuracy, args.rb)
+                not args.no_cpu, args.cpu_budget, not args.no_accuracy, (2 if args.rb and args.rb_precond else 1 if args.rb else 0))
     if rank != 0:
         return
     K = args.steps

@@ -54,10 +54,13 @@ extern "C" {
 /* flags */
 #define TBL_FLAG_REPLAY        1  /* follow counts given by tbl_set_replay instead of testing convergence */
 #define TBL_FLAG_PPE_RESIDUAL  2  /* compute the true relative PPE residual after each solve */
-#define TBL_FLAG_RB_ORDER      8  /* throughput mode, not the reference's arithmetic: red-black (i+j+k odd/even)
-                                     ordering of the implicit-diffusion Gauss-Seidel sweeps and of the SSOR
-                                     preconditioner (one global block, periodic in j), so every sweep is two
-                                     fully parallel passes; the converged solves are the same */
+#define TBL_FLAG_RB_ORDER      8  /* throughput mode, not the reference's sweep order: red-black (i+j+k odd/even)
+                                     ordering of the implicit-diffusion Gauss-Seidel sweeps (one global block,
+                                     periodic in j), so every sweep is two fully parallel passes; the converged
+                                     solves are the same systems */
+#define TBL_FLAG_RB_PRECOND   16  /* with TBL_FLAG_RB_ORDER: the SSOR preconditioner of GMRES red-black ordered
+                                     too.  A weaker preconditioner (about 2.7x the GMRES iterations at
+                                     512x128x128), kept for experiments */
 #define TBL_FLAG_DIAGNOSTICS   4  /* accepted for compatibility: the divergence, mass-flux, wall-shear and
                                      KE diagnostics run every step, as in the reference */
 

@@ -40,6 +40,7 @@ TBL_FLAG_REPLAY = 1
 TBL_FLAG_PPE_RESIDUAL = 2
 TBL_FLAG_DIAGNOSTICS = 4
 TBL_FLAG_RB_ORDER = 8
+TBL_FLAG_RB_PRECOND = 16
 
 TBL_BRANCH_FREE = 0
 TBL_BRANCH_RECORD = 1

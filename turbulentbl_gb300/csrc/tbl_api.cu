@@ -641,6 +641,7 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
         return TBL_ERR_BAD_ARG;
     if (cfg->precision == TBL_PREC_MIXED && (cfg->flags & TBL_FLAG_REPLAY)) return TBL_ERR_BAD_ARG;
     if ((cfg->flags & TBL_FLAG_RB_ORDER) && ((cfg->ny - 2) % 2 != 0)) return TBL_ERR_BAD_ARG;  // colouring vs wrap
+    if ((cfg->flags & TBL_FLAG_RB_PRECOND) && !(cfg->flags & TBL_FLAG_RB_ORDER)) return TBL_ERR_BAD_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TBL_ERR_NO_DEVICE;
     tbl_handle* h = new (std::nothrow) tbl_handle();

@@ -460,7 +460,14 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const T* __restrict__ pc
 // Throughput mode, not the reference's arithmetic.  Points are coloured by
 // the parity of i+j+k (the number of unique span rows is even, so the
 // periodic wrap keeps the colouring); every neighbour of a point has the other
-// colour, so a colour pass updates all its points at once.
+// colour, so a colour pass updates all its points at once.  Threads map onto
+// the points of the pass's colour only (i = rb_i0 + 2t along a row), so no
+// lane of a warp idles: the FP64 passes are bound by FP64 issue, which a warp
+// pays in full however many of its lanes are active.
+
+// First interior i of colour `color` on row (j, k): i + j + k has the
+// colour's parity.
+__device__ __forceinline__ int rb_i0(int color, int j, int k) { return 2 - ((color + j + k) & 1); }
 
 // Gauss-Seidel half sweep of the listed components over one colour, the whole
 // domain as one block (no slab halos), periodic in j:
@@ -469,11 +476,11 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const T* __restrict__ pc
 template <typename T>
 __global__ void __launch_bounds__(256) k_rb_gs(Geom g, const T* __restrict__ pc, const T* __restrict__ pbv,
                                                Ptr3<T> Fs, Ptr3<T> Qs, int c0_, int c1_, int c2_, int color) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y;
     const int K = g.nz - 2;
     const int ci = blockIdx.z / K, k = 1 + blockIdx.z % K;
-    if (i > g.nx - 2 || ((i + j + k) & 1) != color) return;
+    const int i = rb_i0(color, j, k) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i > g.nx - 2) return;
     const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
     T* F = const_cast<T*>(Fs.p[comp]);
     const int nz = g.nz;
@@ -497,10 +504,10 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_rb_ssor(Geom g, T aw, T as, const T* __restrict__ Ab,
                                                  const T* __restrict__ At, const T* __restrict__ sk, T cfac,
                                                  const T* __restrict__ RH, T* __restrict__ OUT, int pass) {
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     const int color = pass == 1 ? 1 : 0;
-    if (i > g.nx - 2 || ((i + j + k) & 1) != color) return;
+    const int i = rb_i0(color, j, k) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i > g.nx - 2) return;
     const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
     const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
     const long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
@@ -631,7 +638,7 @@ static int rb_gs(tbl_handle* h, T* const F[3], const T* const Q[3], const T* pc,
     const Geom& g = h->g;
     Ptr3<T> Fs, Qs;
     for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; }
-    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
+    dim3 grid(((g.nx - 1) / 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
     for (int color = 0; color < 2; ++color)
         k_rb_gs<T><<<grid, 256, 0, h->stream>>>(g, pc, pb, Fs, Qs, comps[0], ncomp > 1 ? comps[1] : 0,
                                                 ncomp > 2 ? comps[2] : 0, color);
@@ -680,7 +687,7 @@ int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
         g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
         h->lap_scale);
     h->launches++;
-    if (h->cfg.flags & TBL_FLAG_RB_ORDER) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
+    if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     return launch_sweep<SW_FWD, double>(h, a, 1);
@@ -691,7 +698,7 @@ static int rb_ssor(tbl_handle* h, T aw, T as, const T* Ab, const T* At, const T*
     const Geom& g = h->g;
     const double w = h->cfg.omega;
     const T cfac = (T)(-w * ((2.0 - w) / w));
-    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
+    dim3 grid(((g.nx - 1) / 2 + 255) / 256, g.ny - 2, g.nz - 2);  // (nx-1)/2 >= the points of a colour on a row
     k_rb_ssor<T><<<grid, 256, 0, h->stream>>>(g, aw, as, Ab, At, sk, cfac, RH, out, 1);
     k_rb_ssor<T><<<grid, 256, 0, h->stream>>>(g, aw, as, Ab, At, sk, cfac, RH, out, 2);
     h->launches += 2;
@@ -699,7 +706,7 @@ static int rb_ssor(tbl_handle* h, T aw, T as, const T* Ab, const T* At, const T*
 }
 
 int launch_ssor_bwd(tbl_handle* h, double* out) {
-    if (h->cfg.flags & TBL_FLAG_RB_ORDER)
+    if (h->cfg.flags & TBL_FLAG_RB_PRECOND)
         return rb_ssor<double>(h, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At,
                                h->lap_scale, h->RH, out);
     SweepArgs<double> a = base_args<double>(h);
@@ -722,14 +729,14 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
                                                                 h->coef_f + g.nz, h->coef_f + 2 * (size_t)g.nz, Xf,
                                                                 nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz);
     h->launches++;
-    if (h->cfg.flags & TBL_FLAG_RB_ORDER) return TBL_OK;
+    if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
     return launch_sweep<SW_FWD, float>(h, a, 1);
 }
 
 int launch_ssor_bwd_f(tbl_handle* h, float* out) {
-    if (h->cfg.flags & TBL_FLAG_RB_ORDER) {
+    if (h->cfg.flags & TBL_FLAG_RB_PRECOND) {
         const size_t nz = (size_t)h->g.nz;
         return rb_ssor<float>(h, (float)(1.0 / (h->cfg.dx * h->cfg.dx)), (float)(1.0 / (h->cfg.dy * h->cfg.dy)),
                               h->coef_f, h->coef_f + nz, h->coef_f + 3 * nz, h->RHf, out);
