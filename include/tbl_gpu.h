@@ -51,6 +51,29 @@ extern "C" {
 #define TBL_PREC_FP64   0   /* the plain method: every field and operation in FP64 */
 #define TBL_PREC_MIXED  1   /* FP32 stencils/storage/inner GMRES inside FP64 iterative refinement */
 
+/* Variants: the reference's three programs of the same method.  Their
+ * differences on the time step are switched by tbl_config.variant; cum,
+ * recycle_after and nproc stay separate parameters (originalTBL: 1000 and
+ * 1000, dnssetbl: freqTimAvg = 500 for both).  Adjoint windows and the
+ * red-black mode take TBL_VARIANT_DNSTBL2 only. */
+#define TBL_VARIANT_DNSTBL2   0  /* dnstbl2/dnstbl.f90 (default) */
+#define TBL_VARIANT_ORIGINAL  1  /* originalTBL/fnldnstbl.f90: Peclet windows Pe > 2 without the upper bounds
+                                    (:665, :689, :711); inflow u mean ramped from Ume1 to the recycled mean,
+                                    eps = min(cnt2 * 5e-5, 1) with cnt2 = tbl_state.cnt2 (:561-587, :2382);
+                                    divergence print sqrt(|sum|/N) (:1586); wall-shear window 1000 steps
+                                    (:1679-1681) */
+#define TBL_VARIANT_DNSSETBL  2  /* dnssetbl/dnssetbl.f90: Pe = |Re u h| > 2 (:311, :323, :335); second-order
+                                    central y convection on the first/last span rows (:325-326); inflow
+                                    eps = min(nstep * 5e-5, 1) ramp of the u mean, v mean times lamda, blend
+                                    weight Wt(1,k) (:259-300); Gauss-Seidel also stops when the L1 residual
+                                    sum < 1e-12 (a REAL(4) literal, :392); slabs nz/P from k = 1 with the
+                                    remainder on the last ranks (:78-92); unweighted span statistics
+                                    (:936-983); rescaling when mod(nstep, cum) = 0 (:986) with the recycled
+                                    plane refreshed on rank 0's slab (:1033-1041); fluctuations and KE when
+                                    cont > recycle_after over i = 2..nx-1 (:1223-1254); mass flux over each
+                                    slab's own planes, divided by (x3(nz-1)-x3(2))(x2(ny-1)-x2(2))
+                                    (:884-896) */
+
 /* flags */
 #define TBL_FLAG_REPLAY        1  /* follow counts given by tbl_set_replay instead of testing convergence */
 #define TBL_FLAG_PPE_RESIDUAL  2  /* compute the true relative PPE residual after each solve */
@@ -89,6 +112,8 @@ typedef struct tbl_config {
     double mixed_inner_tol; /* inner FP32 GMRES relative tolerance (mixed mode) */
     double mixed_outer_tol; /* FP64 refinement residual target, relative (mixed mode) */
     double mixed_true_tol;  /* mixed mode: also refine until ||Q8 - L7 p'||_2 / ||Q8||_2 <= this (0 = off) */
+    int32_t variant;        /* TBL_VARIANT_*: which of the reference's programs the step follows */
+    int32_t reserved_;      /* zero */
 } tbl_config;
 
 /* Mesh, host-computed once (dnstbl2/dnstbl.f90:392-426): x1(nx), x2(ny),
@@ -119,7 +144,8 @@ typedef struct tbl_state {
     int32_t nstep;                          /* from the 3D.tp header */
     int32_t cont;                           /* steps since program start (drives cum) */
     int32_t ksep;                           /* last inner index of the previous rescaling */
-    int32_t pad_;
+    int32_t cnt2;                           /* steps this program has run (originalTBL's cnt2, :143 :2382);
+                                               drives TBL_VARIANT_ORIGINAL's inflow ramp */
 } tbl_state;
 
 /* Per-step report (replaces the reference's stdout/ASCII monitors). */

@@ -42,6 +42,10 @@ TBL_FLAG_DIAGNOSTICS = 4
 TBL_FLAG_RB_ORDER = 8
 TBL_FLAG_RB_PRECOND = 16
 
+TBL_VARIANT_DNSTBL2 = 0
+TBL_VARIANT_ORIGINAL = 1
+TBL_VARIANT_DNSSETBL = 2
+
 TBL_BRANCH_FREE = 0
 TBL_BRANCH_RECORD = 1
 TBL_BRANCH_REPLAY = 2
@@ -61,6 +65,7 @@ class TblConfig(C.Structure):
         ("dx", C.c_double), ("dy", C.c_double), ("dxi", C.c_double),
         ("omega", C.c_double), ("errtol", C.c_double), ("errorstop", C.c_double),
         ("mixed_inner_tol", C.c_double), ("mixed_outer_tol", C.c_double), ("mixed_true_tol", C.c_double),
+        ("variant", C.c_int32), ("reserved_", C.c_int32),
     ]
 
 
@@ -75,7 +80,7 @@ class TblState(C.Structure):
         ("uf", _dp), ("vf", _dp), ("wf", _dp), ("newk", _ip), ("ume1", _dp),
         ("bltkns", _dp),
         ("lamda", C.c_double), ("time", C.c_double),
-        ("nstep", C.c_int32), ("cont", C.c_int32), ("ksep", C.c_int32), ("pad_", C.c_int32),
+        ("nstep", C.c_int32), ("cont", C.c_int32), ("ksep", C.c_int32), ("cnt2", C.c_int32),
     ]
 
 

@@ -109,6 +109,21 @@ class RunParams:
     mixed_inner_tol: float = 1.0e-5
     mixed_outer_tol: float = 1.0e-10
     mixed_true_tol: float = 1.0e-8   # divergence target of the mixed solve (true relative PPE residual)
+    variant: int = 0                 # TBL_VARIANT_*: dnstbl2 (0), originalTBL (1), dnssetbl (2)
+
+    def use_variant(self, variant):
+        """Switch to one of the reference's programs with its own cum and
+        recycling start: originalTBL cum = 1000, recycling after step 1000
+        (fnldnstbl.f90:115, :567); dnssetbl freqTimAvg = 500 for both
+        (dnssetbl.f90:20, :264, :986)."""
+        self.variant = variant
+        if variant == 1:
+            self.cum, self.recycle_after = 1000, 1000
+        elif variant == 2:
+            self.cum, self.recycle_after = 500, 500
+        else:
+            self.cum, self.recycle_after = 5, 5
+        return self
 
 
 def recycle_plane(nx):
@@ -141,6 +156,7 @@ def make_config(mesh, rp):
     c.mixed_inner_tol = rp.mixed_inner_tol
     c.mixed_outer_tol = rp.mixed_outer_tol
     c.mixed_true_tol = rp.mixed_true_tol
+    c.variant = rp.variant
     return c
 
 

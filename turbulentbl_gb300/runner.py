@@ -78,6 +78,7 @@ class AbiRunner:
         s.nstep = int(state.get("nstep", 0))
         s.cont = int(state.get("cont", 0))
         s.ksep = int(state.get("ksep", 0))
+        s.cnt2 = int(state.get("cnt2", 0))
         st = self._fn("upload_state")(self._h, C.byref(s))
         if st != abi.TBL_OK:
             raise TblError(st, self.prefix + "upload_state")
@@ -104,7 +105,7 @@ class AbiRunner:
         if st != abi.TBL_OK:
             raise TblError(st, self.prefix + "download_state")
         out.update(newk=newk, ume1=ume1, bltkns=bl, lamda=s.lamda, time=s.time, nstep=s.nstep,
-                   cont=s.cont, ksep=s.ksep)
+                   cont=s.cont, ksep=s.ksep, cnt2=s.cnt2)
         return out
 
     def download_stats(self):
