@@ -6,6 +6,8 @@ is written separately from the C++ code (array slicing for the stencils,
 explicit loops only where the reference is sequential: GS, SSOR, the
 rescaling scans).  Follows theparvezahmad/turbulentBL dnstbl2/dnstbl.f90; the
 line ranges are cited per function.  Arrays are indexed [i, j, k] 0-based.
+``rp.variant`` switches to the differences of originalTBL/fnldnstbl.f90 (1)
+and dnssetbl/dnssetbl.f90 (2), cited where applied.
 Parity status: unpinned against the reference binary (no Fortran compiler).
 """
 import numpy as np
@@ -18,13 +20,23 @@ class NpOracle:
         nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
         self.nx, self.ny, self.nz = nx, ny, nz
         P = rp.nproc
-        loc = (nz - 1) // P
-        # 0-based slabs [bn, en] (dnstbl2/dnstbl.f90:469-475)
+        self.var = getattr(rp, "variant", 0)
         self.slabs = []
-        for r in range(P):
-            bn = 1 + r * loc
-            en = bn + loc - 1 if r < P - 1 else nz - 2
-            self.slabs.append((bn, en))
+        if self.var == 2:
+            # dnssetbl.f90:78-92: sizes nz//P, the last nz % P ranks one more,
+            # from the first plane; the wall and top planes are then dropped
+            sizes = [nz // P + (1 if r >= P - nz % P else 0) for r in range(P)]
+            starts = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+            for r in range(P):
+                self.slabs.append((int(starts[r]) + (1 if r == 0 else 0),
+                                   int(starts[r] + sizes[r] - 1) - (1 if r == P - 1 else 0)))
+        else:
+            loc = (nz - 1) // P
+            # 0-based slabs [bn, en] (dnstbl2/dnstbl.f90:469-475)
+            for r in range(P):
+                bn = 1 + r * loc
+                en = bn + loc - 1 if r < P - 1 else nz - 2
+                self.slabs.append((bn, en))
         self.dx, self.dy, self.dxi = mesh.dx, mesh.dy, mesh.dxi
         J = mesh.jac
         self.jinv = 1.0 / J
@@ -56,6 +68,9 @@ class NpOracle:
         self.fl_file = [np.array(uf[c][ir]) if uf[c] is not None else self.U[c][ir] - means[c][ir][None, :]
                         for c in range(3)]
         self.fl_live = [f.copy() for f in self.fl_file]
+        if self.var == 2:  # computed on each rank's own slab only (dnssetbl.f90:141-149)
+            self.fl_file = [np.zeros_like(f) for f in self.fl_file]
+        self.cnt2 = st.get("cnt2", 0)
         self.lamda = st.get("lamda", 1.0)
         self.nstep = st.get("nstep", 0)
         self.cont = st.get("cont", 0)
@@ -78,14 +93,28 @@ class NpOracle:
             if self.usum2[ir, k] < 0.99 * ue:
                 nk = self.newk[k] - 1
                 src = self.fl_live if bn <= nk <= en else self.fl_file
-                wt = self.Wt[nx - 2, k]
-                means = (self.ume1[k], self.vsum2[ir, nk], self.wsum2[ir, nk])
+                wt = self.Wt[0 if self.var == 2 else nx - 2, k]  # dnssetbl: Wt(1,k) (dnssetbl.f90:291)
+                um = self.ume1[k]
+                if self.var:  # eps ramp (fnldnstbl.f90:561-587, dnssetbl.f90:259-274)
+                    eps = min((self.cnt2 if self.var == 1 else self.nstep) * 5.0e-5, 1.0)
+                    um = eps * self.usum2[ir, nk] + (1 - eps) * self.ume1[k]
+                vm = self.lamda * self.vsum2[ir, nk] if self.var == 2 else self.vsum2[ir, nk]
+                means = (um, vm, self.wsum2[ir, nk])
                 for c in range(3):
                     f = self.lamda * src[c][1:ny - 1, nk]
                     self.U[c][0, 1:ny - 1, k] = (means[c] + f) * (1.0 - wt) + (means[c] + f) * wt
             else:
                 for c, s in enumerate((self.usum2, self.vsum2, self.wsum2)):
                     self.U[c][0, 1:ny - 1, k] = s[ir, k]
+
+    def _win(self, Pe, hi):
+        """Peclet window: 2 < Pe < hi; originalTBL Pe > 2 (fnldnstbl.f90:665);
+        dnssetbl |Pe| > 2 (dnssetbl.f90:311)."""
+        if self.var == 2:
+            return np.abs(Pe) > 2
+        if self.var == 1:
+            return Pe > 2
+        return (Pe > 2) & (Pe < hi)
 
     # a2, a3: convection and Q (:621-768)
     def conv_q(self):
@@ -114,7 +143,7 @@ class NpOracle:
             t1 = np.abs(uc) * (fp2 - 4 * fp1 + 6 * f0 - 4 * fm1 + fm2) * (0.25 / self.dx)
             t2 = uc * (-fp2 + 8 * fp1 - 8 * fm1 + fm2) * (c12 / self.dx)
             cen = uc * ((fm2 - 8 * fm1 + 8 * fp1 - fp2) * (c12 / self.dx))
-            d1 = np.where(near, dn, np.where((Pe > 2) & (Pe < 50), t1 + t2, cen))
+            d1 = np.where(near, dn, np.where(self._win(Pe, 50), t1 + t2, cen))
             # y (periodic, first-order upwind on the first/last unique rows)
             gm1, gp1 = F[ii, self.jm1[jj], kk], F[ii, self.jp1[jj], kk]
             gm2, gp2 = F[ii, self.jm2[jj], kk], F[ii, self.jp2[jj], kk]
@@ -124,7 +153,9 @@ class NpOracle:
             t1 = np.abs(vc) * (gp2 - 4 * gp1 + 6 * f0 - 4 * gm1 + gm2) * (0.25 / self.dy)
             t2 = vc * (-gp2 + 8 * gp1 - 8 * gm1 + gm2) * (c12 / self.dy)
             cen = vc * ((gm2 - 8 * gm1 + 8 * gp1 - gp2) * (c12 / self.dy))
-            d2 = np.where(near, up, np.where((Pe > 2) & (Pe < 50), t1 + t2, cen))
+            if self.var == 2:  # central on the first/last rows (dnssetbl.f90:325-326)
+                up = vc * (gp1 - gm1) * (0.5 / self.dy)
+            d2 = np.where(near, up, np.where(self._win(Pe, 50), t1 + t2, cen))
             # xi
             hm1, hp1 = F[ii, jj, kk - 1], F[ii, jj, kk + 1]
             hm2 = F[ii, jj, np.maximum(kk - 2, 0)]
@@ -135,7 +166,7 @@ class NpOracle:
             t1 = np.abs(wc) * (hp2 - 4 * hp1 + 6 * f0 - 4 * hm1 + hm2) * (0.25 / self.dxi)
             t2 = wc * (-hp2 + 8 * hp1 - 8 * hm1 + hm2) * (c12 / self.dxi)
             cen = wc * ((hm2 - 8 * hm1 + 8 * hp1 - hp2) * (c12 / self.dxi))
-            d3 = np.where(near, dn, np.where((Pe > 2) & (Pe < 5), t1 + t2, cen))
+            d3 = np.where(near, dn, np.where(self._win(Pe, 5), t1 + t2, cen))
             conv.append(d1 + d2 + d3 * self.jinv[kk])
         P = self.P
         g1 = 0.5 * (P[ii + 1, jj, kk] - P[ii - 1, jj, kk]) / self.dx
@@ -171,7 +202,8 @@ class NpOracle:
                     if it == 1:
                         sumnor = 1.0 / diver
                     sumav = diver * sumnor
-                    stop = (n >= target[c]) if target is not None else (sumav < self.rp.errorstop)
+                    stop = (n >= target[c]) if target is not None else (
+                        sumav < self.rp.errorstop or (self.var == 2 and diver < float(np.float32(1e-12))))
                     if stop:
                         break
                 old = F.copy()  # neighbours' halo planes as of the previous sweep
@@ -354,17 +386,24 @@ class NpOracle:
             F[:, 0, :] = F[:, ny - 2, :]
             F[:, ny - 1, :] = F[:, 1, :]
 
-    # a9 (:1707-1993)
+    # a9 (:1707-1722): the recycled plane refreshed on every slab
+    def fluc(self, run_steps):
+        ny, nz, ir = self.ny, self.nz, self.rp.irec - 1
+        on = (run_steps > self.rp.recycle_after) if self.var == 2 else (self.nstep > self.rp.recycle_after)
+        if on:
+            for c, mn in enumerate((self.usum2, self.vsum2, self.wsum2)):
+                self.fl_live[c][1:ny - 1, 1:nz - 1] = self.U[c][ir, 1:ny - 1, 1:nz - 1] - mn[ir, 1:nz - 1][None, :]
+
+    # a9 (:1881-1993); dnssetbl unweighted / (ny-2) (dnssetbl.f90:936-983)
     def stats(self):
         nx, ny, nz, ir = self.nx, self.ny, self.nz, self.rp.irec - 1
         u, v, w = self.U
-        if self.nstep > self.rp.recycle_after:
-            for c, mn in enumerate((self.usum2, self.vsum2, self.wsum2)):
-                self.fl_live[c][1:ny - 1, 1:nz - 1] = self.U[c][ir, 1:ny - 1, 1:nz - 1] - mn[ir, 1:nz - 1][None, :]
         self.cont += 1
         if self.nstep % self.rp.istat == 0:
             A = self.m.x2[ny - 1] - self.m.x2[1]
             dA = self.dy
+            if self.var == 2:
+                A, dA = float(ny - 2), 1.0
             jj = np.arange(1, ny - 1)
             su = 0.5 * (u[:, jj, :] + u[:, self.jp1[jj], :])
             sv = 0.5 * (v[:, jj, :] + v[:, self.jp1[jj], :])
@@ -386,8 +425,9 @@ class NpOracle:
         self.lamda = utau1 / utau2
         bl, wt, newk, ksep = rescaling_state(self.usum2, x3, ue, self.rp.irec, self.lamda, self.ksep, self.bltkns)
         self.bltkns, self.Wt, self.newk, self.ksep = bl, wt, newk, ksep
+        k0, k1 = self.slabs[0] if self.var == 2 else (1, nz - 2)  # dnssetbl: rank 0's slab (dnssetbl.f90:1033)
         for c, mn in enumerate((self.usum2, self.vsum2, self.wsum2)):
-            self.fl_live[c][1:ny - 1, 1:nz - 1] = self.U[c][ir, 1:ny - 1, 1:nz - 1] - mn[ir, 1:nz - 1][None, :]
+            self.fl_live[c][1:ny - 1, k0:k1 + 1] = self.U[c][ir, 1:ny - 1, k0:k1 + 1] - mn[ir, k0:k1 + 1][None, :]
         for k in self.sums:
             self.sums[k][:] = 0.0
 
@@ -401,7 +441,15 @@ class NpOracle:
         self.div()
         kits = self.gmres(None if counts is None else counts[3:])
         self.project_bcs(uold1)
-        self.stats()
-        if self.cont % self.rp.cum == 0:
-            self.rescale()
+        if self.var == 2:  # statistics, rescaling on nstep, then the fluctuations (dnssetbl.f90:936, :986, :1223)
+            self.stats()
+            if self.nstep % self.rp.cum == 0:
+                self.rescale()
+            self.fluc(self.cont)
+        else:
+            self.fluc(self.cont + 1)
+            self.stats()
+            if self.cont % self.rp.cum == 0:
+                self.rescale()
+        self.cnt2 += 1
         return sweeps + [len(kits)] + kits

@@ -23,6 +23,11 @@
  * Floating-point expression order follows the Fortran source (left to right,
  * no contraction: build with -ffp-contract=off).
  *
+ * tbl_config.variant switches to the differences of the reference's other
+ * two programs of the method, originalTBL/fnldnstbl.f90 and
+ * dnssetbl/dnssetbl.f90 (each cited where it is applied); everything else
+ * follows dnstbl2.
+ *
  * Parity status: UNPINNED against the reference binary.  No Fortran compiler
  * or MPI exists on either build machine, and the reference ships no tests,
  * golden vectors or input files.  The restatement is pinned instead by an
@@ -63,7 +68,7 @@ struct Oracle {
     bool fluc_updated = false;
     std::vector<int> newk;
     double lamda = 1.0, lamda03 = 0, time = 0;
-    int nstep = 0, cont = 0, ksep = 0, nstat = 0;
+    int nstep = 0, cont = 0, ksep = 0, nstat = 0, cnt2 = 0;
     // statistics
     std::vector<double> usum, vsum, wsum, uusum, vvsum, wwsum, uvsum, uwsum, vwsum;
     std::vector<double> deltastar, theta, Ht, Reth, sumxz, tauw_window;
@@ -93,6 +98,9 @@ struct Oracle {
     }
 };
 
+inline bool is_orig(const Oracle& o) { return o.c.variant == TBL_VARIANT_ORIGINAL; }
+inline bool is_sete(const Oracle& o) { return o.c.variant == TBL_VARIANT_DNSSETBL; }
+
 inline double fsign_ceil(double u) {
     // sgn = sign(1, ceiling(u)) (dnstbl2/dnstbl.f90:651): +1 when ceiling(u) >= 0
     return std::ceil(u) >= 0.0 ? 1.0 : -1.0;
@@ -105,14 +113,33 @@ int setup(Oracle& o, const tbl_config* cfg, const tbl_mesh* m) {
     if (cfg->irec < 2 || cfg->irec > o.nx - 1 || cfg->cum < 1 || cfg->istat < 1) return TBL_ERR_BAD_ARG;
     if (cfg->kmax < 1 || cfg->mmax < 1) return TBL_ERR_BAD_ARG;
     o.N = (size_t)o.nx * o.ny * o.nz;
-    // partition (:469-475)
-    int loc_n = (o.nz - 1) / o.P;
-    if (loc_n < 3) return TBL_ERR_BAD_ARG;
+    if (cfg->variant < TBL_VARIANT_DNSTBL2 || cfg->variant > TBL_VARIANT_DNSSETBL) return TBL_ERR_BAD_ARG;
     o.bn.resize(o.P); o.en.resize(o.P);
-    for (int r = 0; r < o.P; ++r) {
-        o.bn[r] = 2 + r * loc_n;
-        o.en[r] = o.bn[r] + loc_n - 1;
-        if (r == o.P - 1) o.en[r] = o.nz - 1;
+    if (cfg->variant == TBL_VARIANT_DNSSETBL) {
+        // dnssetbl.f90:78-92: blocks of nz/P over k = 1..nz, one more point on
+        // the last mod(nz,P) ranks; the first and last planes are boundaries
+        int it1 = o.nz / o.P;
+        const int it2 = o.P - o.nz % o.P;
+        int b = 1;
+        for (int r = 0; r < o.P; ++r) {
+            if (r == it2) it1 = it1 + 1;
+            o.bn[r] = b;
+            o.en[r] = b + it1 - 1;
+            b = o.en[r] + 1;
+        }
+        o.bn[0] = o.bn[0] + 1;
+        o.en[o.P - 1] = o.en[o.P - 1] - 1;
+        for (int r = 0; r < o.P; ++r)
+            if (o.en[r] - o.bn[r] + 1 < 3) return TBL_ERR_BAD_ARG;
+    } else {
+        // partition (:469-475)
+        int loc_n = (o.nz - 1) / o.P;
+        if (loc_n < 3) return TBL_ERR_BAD_ARG;
+        for (int r = 0; r < o.P; ++r) {
+            o.bn[r] = 2 + r * loc_n;
+            o.en[r] = o.bn[r] + loc_n - 1;
+            if (r == o.P - 1) o.en[r] = o.nz - 1;
+        }
     }
     o.x1.assign(m->x1, m->x1 + o.nx);
     o.x2.assign(m->x2, m->x2 + o.ny);
@@ -167,19 +194,31 @@ int setup(Oracle& o, const tbl_config* cfg, const tbl_mesh* m) {
 }
 
 // ---------------------------------------------------------------- a1: inflow
-// dnstbl2/dnstbl.f90:557-618
+// dnstbl2/dnstbl.f90:557-618.  originalTBL ramps the u mean from Ume1 to the
+// recycled mean with eps = min(cnt2 * 5e-5, 1) (fnldnstbl.f90:561-587);
+// dnssetbl ramps it with eps = min(nstep * 5e-5, 1), scales the v mean by
+// lamda and blends with Wt(1,k) (dnssetbl.f90:259-300).
+double inflow_eps(const Oracle& o) {
+    double eps = (is_orig(o) ? (double)o.cnt2 : (double)o.nstep) * (5.0e-5);
+    if (eps > 1.0) eps = 1.0;
+    return eps;
+}
+
 void inflow(Oracle& o) {
     const int irec = o.c.irec, nx = o.nx, ny = o.ny;
+    const bool ramp = is_orig(o) || is_sete(o);
+    const double eps = inflow_eps(o);
     for (int rk = 0; rk < o.P; ++rk) {
         for (int k = o.bn[rk]; k <= o.en[rk]; ++k) {
             if (o.usum2[o.id2(irec, k)] < (0.99 * o.c.ue)) {
                 int nk = o.newk[k - 1];
-                double uin = o.ume1[k - 1];
-                double vin = o.vsum2[o.id2(irec, nk)];
+                double uin = ramp ? eps * (o.usum2[o.id2(irec, nk)]) + (1 - eps) * o.ume1[k - 1] : o.ume1[k - 1];
+                double vin = is_sete(o) ? o.lamda * o.vsum2[o.id2(irec, nk)] : o.vsum2[o.id2(irec, nk)];
                 double win = o.wsum2[o.id2(irec, nk)];
                 bool live = (nk >= o.bn[rk] && nk <= o.en[rk]);
-                // the redundant i loop leaves Wt(nX-1,k) in effect (:594-600)
-                double wt = o.Wt[o.id2(nx - 1, k)];
+                // the redundant i loop leaves Wt(nX-1,k) in effect (:594-600);
+                // dnssetbl uses Wt(1,k) (dnssetbl.f90:291-293)
+                double wt = o.Wt[o.id2(is_sete(o) ? 1 : nx - 1, k)];
                 for (int j = 2; j <= ny - 1; ++j) {
                     double f[3];
                     for (int cc = 0; cc < 3; ++cc) {
@@ -203,6 +242,15 @@ void inflow(Oracle& o) {
 
 // ------------------------------------------------------- a2+a3: conv and Q
 // dnstbl2/dnstbl.f90:621-768
+// Peclet windows: dnstbl2 2 < Pe < 50 (x, y) and 2 < Pe < 5 (xi); originalTBL
+// Pe > 2 (fnldnstbl.f90:665, :689, :711); dnssetbl |Re u h| > 2
+// (dnssetbl.f90:311-345), which equals |Pe| > 2 for the signed Pe here.
+inline bool pe_win(const Oracle& o, double Pe, double hi) {
+    if (is_sete(o)) return std::fabs(Pe) > 2.0;
+    if (is_orig(o)) return Pe > 2.0;
+    return Pe > 2.0 && Pe < hi;
+}
+
 void conv_q(Oracle& o) {
     const int nx = o.nx, ny = o.ny, nz = o.nz;
     const double tf = o.c.re, dt = o.c.dt;
@@ -224,7 +272,7 @@ void conv_q(Oracle& o) {
                     Pe = fsign_ceil(u) * tf * u * o.dx;
                     if (i <= 2 || i >= nx - 1) {
                         d1 = u * (F[o.id(ip1, j, k)] - F[o.id(im1, j, k)]) / (2.0 * o.dx);
-                    } else if (Pe > 2.0 && Pe < 50.0) {
+                    } else if (pe_win(o, Pe, 50.0)) {
                         term1 = (std::fabs(u)) *
                                 (F[o.id(ip2, j, k)] - (4 * (F[o.id(ip1, j, k)])) + (6 * (F[o.id(i, j, k)])) -
                                  (4 * (F[o.id(im1, j, k)])) + F[o.id(im2, j, k)]) *
@@ -241,12 +289,15 @@ void conv_q(Oracle& o) {
                     }
                     double v = U2[o.id(i, j, k)];
                     Pe = fsign_ceil(v) * tf * v * o.dy;
-                    if (j == 2 || j == ny - 1) {
+                    if ((j == 2 || j == ny - 1) && is_sete(o)) {
+                        // second-order central on the first/last rows (dnssetbl.f90:325-326)
+                        d2 = v * (F[o.id(i, jp1_, k)] - F[o.id(i, jm1_, k)]) * 0.5 * o.invdy;
+                    } else if (j == 2 || j == ny - 1) {
                         double a1 = std::max(v, 0.0), b = std::min(v, 0.0);
                         term1 = a1 * ((F[o.id(i, j, k)] - F[o.id(i, jm1_, k)]) * (o.invdy));
                         term2 = b * ((F[o.id(i, jp1_, k)] - F[o.id(i, j, k)]) * (o.invdy));
                         d2 = term1 + term2;
-                    } else if (Pe > 2.0 && Pe < 50.0) {
+                    } else if (pe_win(o, Pe, 50.0)) {
                         term1 = (std::fabs(v)) *
                                 (F[o.id(i, jp2_, k)] - (4 * (F[o.id(i, jp1_, k)])) + (6 * (F[o.id(i, j, k)])) -
                                  (4 * (F[o.id(i, jm1_, k)])) + F[o.id(i, jm2_, k)]) *
@@ -265,7 +316,7 @@ void conv_q(Oracle& o) {
                     Pe = (fsign_ceil(w) * tf * w * (o.x3[k] - o.x3[k - 1]));
                     if ((k <= 2) || (k >= nz - 1)) {
                         d3 = (w * (F[o.id(i, j, k + 1)] - F[o.id(i, j, k - 1)]) * (0.5 * o.invdxi));
-                    } else if (Pe > 2.0 && Pe < 5.0) {
+                    } else if (pe_win(o, Pe, 5.0)) {
                         term1 = (std::fabs(w)) *
                                 (F[o.id(i, j, k + 2)] - (4 * (F[o.id(i, j, k + 1)])) + (6 * (F[o.id(i, j, k)])) -
                                  (4 * (F[o.id(i, j, k - 1)])) + F[o.id(i, j, k - 2)]) *
@@ -338,7 +389,10 @@ void gs_solve(Oracle& o, int replay_sweeps[3], int out_sweeps[3], double out_res
                 for (int rk = 0; rk < o.P; ++rk) diver += part[rk];  // allreduce in rank order
                 if (it == 1) sumnor = 1.0 / diver;
                 sumav = diver * sumnor;
-                bool stop = replay ? (sweeps >= replay_sweeps[jc]) : (sumav < o.c.errorstop);
+                // dnssetbl also stops on the absolute sum, res < 1e-12 with a
+                // REAL(4) literal (dnssetbl.f90:392)
+                bool stop = replay ? (sweeps >= replay_sweeps[jc])
+                                   : (sumav < o.c.errorstop || (is_sete(o) && diver < (double)1e-12f));
                 if (stop) break;
             }
             // snapshot the halo planes every rank receives after the previous sweep
@@ -713,22 +767,26 @@ double div_diag(const Oracle& o) {
                 }
         tot += tmp;
     }
-    return std::fabs(tot) / ((double)(ny - 2) * (nx - 2) * (nz - 2));
+    const double q = std::fabs(tot) / ((double)(ny - 2) * (nx - 2) * (nz - 2));
+    return is_orig(o) ? std::sqrt(q) : q;  // originalTBL prints the square root (fnldnstbl.f90:1586)
 }
 
 // Mass flux through five cross-stream planes (:1578-1594): per rank the cell
 // sums over its k range (rank 0 also the first cell layer, the last rank not
 // its top face), ranks summed in order, divided by the area Av (:448).
 // Plane indices are the reference's literals (:95), clamped to nx-1.
+// dnssetbl sums each slab's own planes only and divides by
+// (x3(nz-1)-x3(2))(x2(ny-1)-x2(2)) (dnssetbl.f90:884-896).
 void mass_flux(Oracle& o) {
     static const int plane[5] = {5, 20, 40, 60, 85};
     const int nx = o.nx, ny = o.ny, nz = o.nz;
-    const double Av = o.x3[nz - 1] * (o.x2[ny - 2] - o.x2[1]);
+    const double Av = is_sete(o) ? (o.x3[nz - 2] - o.x3[1]) * (o.x2[ny - 2] - o.x2[1])
+                                 : o.x3[nz - 1] * (o.x2[ny - 2] - o.x2[1]);
     for (int q = 0; q < 5; ++q) {
         const int ip = plane[q] < nx - 1 ? plane[q] : nx - 1;
         double tot = 0.0;
         for (int rk = 0; rk < o.P; ++rk) {
-            const int k0 = rk == 0 ? o.bn[rk] - 1 : o.bn[rk];
+            const int k0 = (rk == 0 && !is_sete(o)) ? o.bn[rk] - 1 : o.bn[rk];
             double ub = 0.0;
             for (int k = k0; k <= o.en[rk]; ++k)
                 for (int j = 2; j <= ny - 1; ++j) {
@@ -769,24 +827,31 @@ void wall_shear(Oracle& o, double* tau_out = nullptr) {
         o.sumxz[i - 1] = tauxz + o.sumxz[i - 1];
     }
     if (tau_out) return;
-    if (o.nstep % 500 == 0) {
-        for (int i = 2; i <= nx - 1; ++i) o.tauw_window[i - 1] = o.sumxz[i - 1] / 500.0;
+    const int win = is_orig(o) ? 1000 : 500;  // originalTBL: 1000 steps (fnldnstbl.f90:1679-1681)
+    if (o.nstep % win == 0) {
+        for (int i = 2; i <= nx - 1; ++i) o.tauw_window[i - 1] = o.sumxz[i - 1] / (double)win;
         for (double& v : o.sumxz) v = 0.0;
     }
 }
 
 // --------------------------------------------------- a9: statistics per step
-// Ufluc per step (:1707-1722), KE (:1724-1741), stats (:1902-1993)
-void per_step_stats(Oracle& o, double& ke, int& blowup) {
+// Ufluc per step (:1707-1722), KE (:1724-1741).  dnssetbl: when
+// cnt > freqTimAvg, cnt counting this run's steps including the current one,
+// over i = 2..nx-1 (dnssetbl.f90:1223-1254; its blow-up test also reads the
+// never-refreshed columns i = 1 and nx, left out here).
+// `run_steps` counts this run's steps including the current one.
+void fluc_ke(Oracle& o, int run_steps, double& ke, int& blowup) {
     const int nx = o.nx, ny = o.ny, nz = o.nz, irec = o.c.irec;
     ke = 0.0; blowup = 0;
-    if (o.nstep > o.c.recycle_after) {
+    const bool on = is_sete(o) ? (run_steps > o.c.recycle_after) : (o.nstep > o.c.recycle_after);
+    const int i0 = is_sete(o) ? 2 : 1, i1 = is_sete(o) ? nx - 1 : nx;
+    if (on) {
         double ke1tot = 0.0;
         for (int rk = 0; rk < o.P; ++rk) {
             double ke1 = 0.0;
             for (int k = o.bn[rk]; k <= o.en[rk]; ++k)
                 for (int j = 2; j <= ny - 1; ++j)
-                    for (int i = 1; i <= nx; ++i) {
+                    for (int i = i0; i <= i1; ++i) {
                         double f1 = o.U[0][o.id(i, j, k)] - o.usum2[o.id2(i, k)];
                         double f2 = o.U[1][o.id(i, j, k)] - o.vsum2[o.id2(i, k)];
                         double f3 = o.U[2][o.id(i, j, k)] - o.wsum2[o.id2(i, k)];
@@ -807,11 +872,19 @@ void per_step_stats(Oracle& o, double& ke, int& blowup) {
         }
         o.fluc_updated = true;
     }
+}
+
+// Statistics (:1902-1993): span averages of the midpoint values weighted
+// dA/A; dnssetbl sums them unweighted and divides by ny-2
+// (dnssetbl.f90:936-983).
+void accumulate_stats(Oracle& o) {
+    const int nx = o.nx, ny = o.ny, nz = o.nz;
     o.cont = o.cont + 1;
     if (o.nstep % o.c.istat == 0) {
         o.nstat += 1;
+        const bool unw = is_sete(o);
         const double dA = o.dy;
-        const double A = o.x2[ny - 1] - o.x2[1];
+        const double A = unw ? (double)(ny - 2) : o.x2[ny - 1] - o.x2[1];
 #pragma omp parallel for schedule(static)
         for (int i = 1; i <= nx; ++i)
             for (int k = 1; k <= nz; ++k) {
@@ -821,6 +894,12 @@ void per_step_stats(Oracle& o, double& ke, int& blowup) {
                     su_ = 0.50 * (o.U[0][o.id(i, j, k)] + o.U[0][o.id(i, jp, k)]);
                     sv_ = 0.50 * (o.U[1][o.id(i, j, k)] + o.U[1][o.id(i, jp, k)]);
                     sw_ = 0.50 * (o.U[2][o.id(i, j, k)] + o.U[2][o.id(i, jp, k)]);
+                    if (unw) {
+                        tu = tu + su_; tv = tv + sv_; tw = tw + sw_;
+                        tuu = tuu + su_ * su_; tvv = tvv + sv_ * sv_; tww = tww + sw_ * sw_;
+                        tuv = tuv + su_ * sv_; tuw = tuw + su_ * sw_; tvw = tvw + sv_ * sw_;
+                        continue;
+                    }
                     tu = tu + (su_ * dA); tv = tv + (sv_ * dA); tw = tw + (sw_ * dA);
                     tuu = tuu + (su_ * su_ * dA); tvv = tvv + (sv_ * sv_ * dA); tww = tww + (sw_ * sw_ * dA);
                     tuv = tuv + (su_ * sv_ * dA); tuw = tuw + (su_ * sw_ * dA); tvw = tvw + (sv_ * sw_ * dA);
@@ -889,8 +968,10 @@ void rescale(Oracle& o) {
         o.Ht[i - 1] = ds / th;
         o.Reth[i - 1] = th * re * ue;
     }
-    // refresh Ufluc(irec,:,k,:) on every rank's own slab (:2341-2349)
-    for (int k = 2; k <= nz - 1; ++k)
+    // refresh Ufluc(irec,:,k,:) on every rank's own slab (:2341-2349);
+    // dnssetbl refreshes rank 0's slab only (dnssetbl.f90:1016, :1033-1041)
+    const int kr0 = is_sete(o) ? o.bn[0] : 2, kr1 = is_sete(o) ? o.en[0] : nz - 1;
+    for (int k = kr0; k <= kr1; ++k)
         for (int j = 2; j <= ny - 1; ++j) {
             o.ufl_live[0][o.idp(j, k)] = o.U[0][o.id(irec, j, k)] - o.usum2[o.id2(irec, k)];
             o.ufl_live[1][o.idp(j, k)] = o.U[1][o.id(irec, j, k)] - o.vsum2[o.id2(irec, k)];
@@ -942,9 +1023,19 @@ int one_step(Oracle& o, tbl_step_stats* st) {
     mass_flux(o);
     wall_shear(o);
     int blow = 0;
-    per_step_stats(o, s.ke, blow);
     s.cum_step = 0;
-    if (o.cont % o.c.cum == 0) { rescale(o); s.cum_step = 1; }
+    if (is_sete(o)) {
+        // dnssetbl: statistics, rescaling every freqTimAvg steps of nstep, then
+        // the fluctuations and KE (dnssetbl.f90:936, :986, :1223)
+        accumulate_stats(o);
+        if (o.nstep % o.c.cum == 0) { rescale(o); s.cum_step = 1; }
+        fluc_ke(o, o.cont, s.ke, blow);
+    } else {
+        fluc_ke(o, o.cont + 1, s.ke, blow);
+        accumulate_stats(o);
+        if (o.cont % o.c.cum == 0) { rescale(o); s.cum_step = 1; }
+    }
+    o.cnt2 = o.cnt2 + 1;  // end of the step (fnldnstbl.f90:2382, dnstbl.f90:2349)
     o.last_counts.clear();
     o.last_counts.push_back(s.gs_sweeps[0]); o.last_counts.push_back(s.gs_sweeps[1]); o.last_counts.push_back(s.gs_sweeps[2]);
     o.last_counts.push_back((int32_t)kits.size());
@@ -1012,8 +1103,11 @@ int orc_upload_state(orc_handle* h, const tbl_state* st) {
         if (uf[cc]) std::memcpy(o.ufl_full_file[cc].data(), uf[cc], o.N * 8);
         else std::fill(o.ufl_full_file[cc].begin(), o.ufl_full_file[cc].end(), 0.0);
     }
+    if (is_sete(o))  // dnssetbl computes the plane on each rank's own slab only: reads elsewhere see zeros
+        for (int cc = 0; cc < 3; ++cc) std::fill(o.ufl_file[cc].begin(), o.ufl_file[cc].end(), 0.0);
     o.fluc_updated = false;
     o.lamda = st->lamda; o.time = st->time; o.nstep = st->nstep; o.cont = st->cont; o.ksep = st->ksep;
+    o.cnt2 = st->cnt2;
     return TBL_OK;
 }
 
@@ -1058,6 +1152,7 @@ int orc_download_state(orc_handle* h, tbl_state* st) {
                 if (k >= 2 && k <= o.nz - 1) uf[cc][o.id(o.c.irec, j, k)] = o.ufl_live[cc][o.idp(j, k)];
     }
     st->lamda = o.lamda; st->time = o.time; st->nstep = o.nstep; st->cont = o.cont; st->ksep = o.ksep;
+    st->cnt2 = o.cnt2;
     return TBL_OK;
 }
 
