@@ -44,7 +44,7 @@ struct Ckpt {
     double* P;
     double* PC;
     double* ufl;  // 3 x (ny, nz) live recycling plane
-    int nstep, cont, nstat;
+    int nstep, cont, nstat, cnt2;
     double time, lamda_host;
     bool fluc;
 };
@@ -804,7 +804,7 @@ int save_ckpt(tbl_handle* h, Ckpt& c) {
     ATRY(dcopy(h, c.P, h->Pr, vol));
     ATRY(dcopy(h, c.PC, h->PC, vol));
     ATRY(dcopy(h, c.ufl, h->ufl_live, 3 * pl));
-    c.nstep = h->nstep; c.cont = h->cont; c.nstat = h->nstat;
+    c.nstep = h->nstep; c.cont = h->cont; c.nstat = h->nstat; c.cnt2 = h->cnt2;
     c.time = h->time; c.lamda_host = h->lamda_host; c.fluc = h->fluc_updated;
     return TBL_OK;
 }
@@ -814,7 +814,7 @@ int restore_ckpt(tbl_handle* h, const Ckpt& c) {
     ATRY(dcopy(h, h->Pr, c.P, vol));
     ATRY(dcopy(h, h->PC, c.PC, vol));
     ATRY(dcopy(h, h->ufl_live, c.ufl, 3 * pl));
-    h->nstep = c.nstep; h->cont = c.cont; h->nstat = c.nstat;
+    h->nstep = c.nstep; h->cont = c.cont; h->nstat = c.nstat; h->cnt2 = c.cnt2;
     h->time = c.time; h->lamda_host = c.lamda_host; h->fluc_updated = c.fluc;
     return TBL_OK;
 }
@@ -930,7 +930,9 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
     if (!h || !wc || nsteps < 1 || wc->ckpt_every < 1) return TBL_ERR_BAD_ARG;
     if (wc->branch_mode < TBL_BRANCH_FREE || wc->branch_mode > TBL_BRANCH_REPLAY) return TBL_ERR_BAD_ARG;
     const tbl_config& c = h->cfg;
-    if (c.precision != TBL_PREC_FP64 || (c.flags & (TBL_FLAG_REPLAY | TBL_FLAG_RB_ORDER))) return TBL_ERR_BAD_ARG;
+    if (c.precision != TBL_PREC_FP64 || (c.flags & (TBL_FLAG_REPLAY | TBL_FLAG_RB_ORDER)) ||
+        c.variant != TBL_VARIANT_DNSTBL2)
+        return TBL_ERR_BAD_ARG;
     for (int s = 1; s <= nsteps; ++s)
         if ((h->cont + s) % c.cum == 0) return TBL_ERR_BAD_ARG;  // a rescaling step inside the window
     std::vector<double> cf;

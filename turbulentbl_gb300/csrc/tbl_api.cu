@@ -131,6 +131,40 @@ static void free_all(tbl_handle* h) {
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
+// 0-based slabs [bn, en] of the P virtual ranks: dnstbl2 loc_n = (nz-1)/P
+// planes each from k = 2, the remainder on the last rank (:469-475); dnssetbl
+// nz/P from k = 1 with one more on the last mod(nz, P) ranks, the wall and
+// top planes left out (dnssetbl.f90:78-92).  False when a slab has fewer than
+// 3 planes.
+bool slab_partition(const tbl_config& c, std::vector<int>& bn, std::vector<int>& en) {
+    const int P = c.nproc, nz = c.nz;
+    if (P < 1) return false;
+    bn.assign(P, 0);
+    en.assign(P, 0);
+    if (c.variant == TBL_VARIANT_DNSSETBL) {
+        int it1 = nz / P, b = 0;
+        const int it2 = P - nz % P;
+        for (int r = 0; r < P; ++r) {
+            if (r == it2) it1 = it1 + 1;
+            bn[r] = b;
+            en[r] = b + it1 - 1;
+            b = en[r] + 1;
+        }
+        bn[0] += 1;
+        en[P - 1] -= 1;
+    } else {
+        const int loc_n = (nz - 1) / P;
+        for (int r = 0; r < P; ++r) {
+            bn[r] = 1 + r * loc_n;
+            en[r] = bn[r] + loc_n - 1;
+            if (r == P - 1) en[r] = nz - 2;
+        }
+    }
+    for (int r = 0; r < P; ++r)
+        if (en[r] - bn[r] + 1 < 3) return false;
+    return true;
+}
+
 static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* h) {
     h->cfg = *cfg;
     const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
@@ -142,14 +176,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     g.J = ny - 2;
     h->npts = (double)nx * ny * nz;
     h->P = cfg->nproc;
-    const int loc_n = (nz - 1) / h->P;  // (:469-475), 1-based bn = 2 + r*loc_n
-    h->bn.resize(h->P);
-    h->en.resize(h->P);
-    for (int r = 0; r < h->P; ++r) {
-        h->bn[r] = 1 + r * loc_n;
-        h->en[r] = h->bn[r] + loc_n - 1;
-        if (r == h->P - 1) h->en[r] = nz - 2;
-    }
+    if (!slab_partition(*cfg, h->bn, h->en)) return TBL_ERR_BAD_ARG;
     TBL_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     {
         int dev = 0;
@@ -220,8 +247,11 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     }
     for (int k = 0; k < nz; ++k) jinv[k] = 1.0 / mesh->jac[k];
     h->x3h = x3;
-    h->stats_A = mesh->x2[ny - 1] - mesh->x2[1];
-    h->area_mf = x3[nz - 1] * (mesh->x2[ny - 2] - mesh->x2[1]);  // Av (:448)
+    const bool sete = cfg->variant == TBL_VARIANT_DNSSETBL;
+    h->stats_dA = sete ? 1.0 : cfg->dy;  // dnssetbl: unweighted span sums over ny-2 (dnssetbl.f90:951-981)
+    h->stats_A = sete ? (double)(ny - 2) : mesh->x2[ny - 1] - mesh->x2[1];
+    h->area_mf = sete ? (x3[nz - 2] - x3[1]) * (mesh->x2[ny - 2] - mesh->x2[1])  // dnssetbl.f90:896
+                      : x3[nz - 1] * (mesh->x2[ny - 2] - mesh->x2[1]);          // Av (:448)
     TBL_CUDA_TRY(cudaMemcpy(h->x3, x3.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->jacinv, jinv.data(), nz * 8, cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMemcpy(h->jac2, j2.data(), nz * 8, cudaMemcpyHostToDevice));
@@ -256,7 +286,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TBL_CUDA_TRY(cudaMemcpy(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice));
     TRY(build_sweep_ctas(h));
     TRY(check_cooperative(h));
-    h->nstep = 0; h->cont = 0; h->nstat = 0; h->time = 0.0;
+    h->nstep = 0; h->cont = 0; h->nstat = 0; h->cnt2 = 0; h->time = 0.0;
     h->fluc_updated = false;
     h->replay_pos = 0;
     h->lamda_host = 1.0;
@@ -297,7 +327,11 @@ int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok)
                 }
                 if (it == 1) sumnor[c] = 1.0 / diver;
                 sumav[c] = diver * sumnor[c];
-                bool stop = target ? (sweeps[c] >= target[c]) : (sumav[c] < h->cfg.errorstop);
+                // dnssetbl also stops on the absolute sum, res < 1e-12 with a
+                // REAL(4) literal (dnssetbl.f90:392)
+                bool stop = target ? (sweeps[c] >= target[c])
+                                   : (sumav[c] < h->cfg.errorstop ||
+                                      (h->cfg.variant == TBL_VARIANT_DNSSETBL && diver < (double)1e-12f));
                 if (stop) active[c] = false;
                 else comps[m++] = c;
             }
@@ -570,30 +604,40 @@ int one_step(tbl_handle* h, tbl_step_stats* out) {
         TRY(launch_project_bcs(h));
     }
     const int nb = red_blocks(h);
-    const bool fluc = h->nstep > c.recycle_after;
+    // dnssetbl: statistics, then the rescaling every cum steps of nstep, then
+    // the fluctuations and KE when this run's step count cnt > recycle_after
+    // (dnssetbl.f90:936, :986, :1223); dnstbl2: fluctuations when
+    // nstep > recycle_after, statistics, rescaling every cum steps of cont
+    // (:1686, :1881, :1974).
+    const bool sete = c.variant == TBL_VARIANT_DNSSETBL;
+    const bool fluc = sete ? (h->cont + 1 > c.recycle_after) : (h->nstep > c.recycle_after);
     {
         ProfScope ps_stats(h, TBL_PROF_STATS, (fluc ? 9.0 : 6.0) * wN);
         TRY(launch_div_diag(h, nb > 512 ? 512 : nb, 3));
         TRY(launch_flux_shear(h));
-        if (fluc) {
+        auto fluc_ke = [&]() -> int {
             TRY(launch_fluc_ke(h, nb > 512 ? 512 : nb, 4));
             const size_t n2 = (size_t)c.nx * c.nz;
             TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl, h->usum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
             TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + n2, h->vsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
             TBL_CUDA_TRY(cudaMemcpyAsync(h->usum2_fl + 2 * n2, h->wsum2, n2 * 8, cudaMemcpyDeviceToDevice, h->stream));
             h->fluc_updated = true;
-        }
+            return TBL_OK;
+        };
+        if (fluc && !sete) TRY(fluc_ke());
         h->cont = h->cont + 1;
         if (h->nstep % c.istat == 0) {
             TRY(launch_stats(h));
             h->nstat++;
         }
         st.cum_step = 0;
-        if (h->cont % c.cum == 0) {
+        if ((sete ? h->nstep : h->cont) % c.cum == 0) {
             TRY(launch_rescale(h));
             st.cum_step = 1;
         }
+        if (fluc && sete) TRY(fluc_ke());
     }
+    h->cnt2 = h->cnt2 + 1;  // end of the step (fnldnstbl.f90:2382, dnstbl.f90:2349)
     // scalars back: red[3] div, red[4] KE, red[5] max fluct, lamda, err
     TRY(readback(h, h->sc, sizeof(DevScalars)));
     if (h->prof_on) TRY(prof_drain(h));
@@ -602,6 +646,7 @@ int one_step(tbl_handle* h, tbl_step_stats* out) {
     int err = 0;
     TBL_CUDA_TRY(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
     st.div_diag = std::fabs(sc.red[3]) / ((double)(c.ny - 2) * (c.nx - 2) * (c.nz - 2));
+    if (c.variant == TBL_VARIANT_ORIGINAL) st.div_diag = std::sqrt(st.div_diag);  // fnldnstbl.f90:1586
     st.ke = fluc ? sc.red[4] / ((double)c.nx * (c.ny - 2) * (c.nz - 2)) : 0.0;
     st.lamda = sc.lamda;
     h->lamda_host = sc.lamda;
@@ -632,7 +677,11 @@ int tbl_create(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle** out) {
     if (!cfg || !mesh || !out || !mesh->x1 || !mesh->x2 || !mesh->x3 || !mesh->jac || !mesh->jac2)
         return TBL_ERR_BAD_ARG;
     if (cfg->nx < 8 || cfg->ny < 6 || cfg->nz < 8 || cfg->nproc < 1) return TBL_ERR_BAD_ARG;
-    if ((cfg->nz - 1) / cfg->nproc < 3) return TBL_ERR_BAD_ARG;
+    if (cfg->variant < TBL_VARIANT_DNSTBL2 || cfg->variant > TBL_VARIANT_DNSSETBL) return TBL_ERR_BAD_ARG;
+    {
+        std::vector<int> b, e;
+        if (!tbl::slab_partition(*cfg, b, e)) return TBL_ERR_BAD_ARG;
+    }
     if (cfg->irec < 2 || cfg->irec > cfg->nx - 1 || cfg->cum < 1 || cfg->istat < 1) return TBL_ERR_BAD_ARG;
     if (cfg->kmax < 1 || cfg->mmax < 1 || !(cfg->dt > 0) || !(cfg->re > 0)) return TBL_ERR_BAD_ARG;
     if (cfg->precision != TBL_PREC_FP64 && cfg->precision != TBL_PREC_MIXED) return TBL_ERR_BAD_ARG;
@@ -703,8 +752,10 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
         if (uf[cc]) TRY(put3(h, h->ufl_full + (size_t)cc * h->g.vol, uf[cc]));
         else TBL_CUDA_TRY(cudaMemsetAsync(h->ufl_full + (size_t)cc * h->g.vol, 0, (size_t)h->g.vol * 8, h->stream));
     }
-    TBL_CUDA_TRY(cudaMemcpyAsync(h->ufl_file, plane.data(), 3 * pl * 8, cudaMemcpyHostToDevice, h->stream));
     TBL_CUDA_TRY(cudaMemcpyAsync(h->ufl_live, plane.data(), 3 * pl * 8, cudaMemcpyHostToDevice, h->stream));
+    if (c.variant == TBL_VARIANT_DNSSETBL)  // computed on each rank's own slab only: reads elsewhere see zeros
+        std::fill(plane.begin(), plane.end(), 0.0);  // (dnssetbl.f90:141-149)
+    TBL_CUDA_TRY(cudaMemcpyAsync(h->ufl_file, plane.data(), 3 * pl * 8, cudaMemcpyHostToDevice, h->stream));
     // scalars
     DevScalars s0;
     TBL_CUDA_TRY(cudaMemcpyAsync(&s0, h->sc, sizeof(s0), cudaMemcpyDeviceToHost, h->stream));
@@ -719,6 +770,7 @@ int tbl_upload_state(tbl_handle* h, const tbl_state* st) {
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->nstep = st->nstep;
     h->cont = st->cont;
+    h->cnt2 = st->cnt2;
     h->time = st->time;
     h->fluc_updated = false;
     h->lamda_host = st->lamda;
@@ -847,6 +899,7 @@ int tbl_download_state(tbl_handle* h, tbl_state* st) {
     st->time = h->time;
     st->nstep = h->nstep;
     st->cont = h->cont;
+    st->cnt2 = h->cnt2;
     return TBL_OK;
 }
 

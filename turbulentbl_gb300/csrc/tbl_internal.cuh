@@ -128,9 +128,10 @@ struct tbl_handle {
     double* bl_out;    // 4 x nx: deltastar theta Ht Reth
     double* ubulk;     // 5: mass flux through the five planes (last step)
     double* sumxz;     // nx: wall-shear accumulator
-    double* tauw_win;  // nx: mean of the last completed 500-step window
-    double area_mf;    // Av = x3(nz) (x2(ny-1) - x2(2)) (1-based)
-    double stats_A;    // x2(ny) - x2(2) (dnstbl2/dnstbl.f90:442)
+    double* tauw_win;  // nx: mean of the last completed wall-shear window
+    double area_mf;    // Av = x3(nz) (x2(ny-1) - x2(2)) (1-based); dnssetbl (x3(nz-1) - x3(2)) (x2(ny-1) - x2(2))
+    double stats_A;    // x2(ny) - x2(2) (dnstbl2/dnstbl.f90:442); dnssetbl ny - 2
+    double stats_dA;   // dy; dnssetbl 1 (unweighted)
     std::vector<double> x3h;  // host copy of x3
     int* slab_of_k;    // nz: slab index of each interior plane
     tbl::DevScalars* sc;
@@ -152,6 +153,7 @@ struct tbl_handle {
     int64_t launches;
     double npts;                   // nx*ny*nz reference points (algorithmic byte counts)
     int nstep, cont, nstat;
+    int cnt2;  // steps this program has run (originalTBL's inflow ramp)
     double time;
     bool fluc_updated;
     int coop_ok;

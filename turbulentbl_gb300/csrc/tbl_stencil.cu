@@ -32,6 +32,10 @@ __global__ void k_save_uold(Geom g, const T* __restrict__ u1, double* __restrict
 }
 
 // Recycling inflow (dnstbl2/dnstbl.f90:557-618).  One thread per (j,k).
+// ramp: the u mean is eps usum2(irec,new(k)) + (1-eps) Ume1(k) (originalTBL
+// fnldnstbl.f90:577, dnssetbl dnssetbl.f90:268); vlam: the v mean is scaled
+// by lamda (dnssetbl.f90:271); wcol: the Wt column of the blend, nx-2 for the
+// redundant i loop (:594-600), 0 for dnssetbl's Wt(1,k) (dnssetbl.f90:291).
 template <typename T>
 __global__ void k_inflow(Geom g, T* __restrict__ u1, T* __restrict__ u2, T* __restrict__ u3,
                          const double* __restrict__ usum2, const double* __restrict__ vsum2,
@@ -39,7 +43,8 @@ __global__ void k_inflow(Geom g, T* __restrict__ u1, T* __restrict__ u2, T* __re
                          const double* __restrict__ ume1, const int* __restrict__ newk,
                          const double* __restrict__ ufl_file, const double* __restrict__ ufl_live,
                          const int* __restrict__ slab_of_k, const SlabDesc* __restrict__ slabs,
-                         const DevScalars* __restrict__ sc, int irec0, double ue) {
+                         const DevScalars* __restrict__ sc, int irec0, double ue, int ramp, double eps, int vlam,
+                         int wcol) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int J = g.ny - 2;
     if (t >= J * (g.nz - 2)) return;
@@ -49,8 +54,9 @@ __global__ void k_inflow(Geom g, T* __restrict__ u1, T* __restrict__ u2, T* __re
     const size_t ir = (size_t)irec0 + (size_t)nx * k;
     if (usum2[ir] < (0.99 * ue)) {
         int nk = newk[k] - 1;  // 0-based source plane
-        double uin = ume1[k];
+        double uin = ramp ? eps * (usum2[(size_t)irec0 + (size_t)nx * nk]) + (1 - eps) * ume1[k] : ume1[k];
         double vin = vsum2[(size_t)irec0 + (size_t)nx * nk];
+        if (vlam) vin = sc->lamda * vin;
         double win = wsum2[(size_t)irec0 + (size_t)nx * nk];
         const SlabDesc s = slabs[slab_of_k[k]];
         bool live = nk >= s.bn && nk < s.bn + s.K;
@@ -59,7 +65,7 @@ __global__ void k_inflow(Geom g, T* __restrict__ u1, T* __restrict__ u2, T* __re
         size_t pj = (size_t)j + (size_t)g.ny * nk;
         double lam = sc->lamda;
         double f1 = lam * src[pj], f2 = lam * src[pl + pj], f3 = lam * src[2 * pl + pj];
-        double w_ = wt[(size_t)(nx - 2) + (size_t)nx * k];  // Wt(nX-1,k): the redundant i loop (:594-600)
+        double w_ = wt[(size_t)wcol + (size_t)nx * k];
         u1[q] = (T)((uin + f1) * (1.0 - w_) + (uin + f1) * w_);
         u2[q] = (T)((vin + f2) * (1.0 - w_) + (vin + f2) * w_);
         u3[q] = (T)((win + f3) * (1.0 - w_) + (win + f3) * w_);
@@ -78,8 +84,22 @@ struct ConvCoef {
     R c12x, c12y, c12z;  // onetwelfth*inv
     R q25x, q25y, q25z;  // 0.25*inv
     R h05z;      // 0.5*invdxi
+    R h05y;      // 0.5*invdy
     R dt;
+    int pe_mode; // Peclet window: 0 dnstbl2 2 < Pe < 50 (5 in xi); 1 originalTBL Pe > 2; 2 dnssetbl |Pe| > 2
+    int ycen;    // 1: central differences on the first/last span rows (dnssetbl.f90:325-326)
 };
+
+// The dissipative window of one direction (hi = 50 in x and y, 5 in xi):
+// dnstbl2 2 < Pe < hi (:655, :679, :701); originalTBL Pe > 2
+// (fnldnstbl.f90:665, :689, :711); dnssetbl |Re u h| > 2 (dnssetbl.f90:311,
+// :323, :335), which is |Pe| > 2 for the signed Pe.
+template <typename R>
+__device__ __forceinline__ bool pe_window(R Pe, R hi, int mode) {
+    if (mode == 2) return abs(Pe) > R(2);
+    if (mode == 1) return Pe > R(2);
+    return Pe > R(2) && Pe < hi;
+}
 
 // Convection of F along x (dnstbl2/dnstbl.f90:651-664)
 template <typename R>
@@ -88,7 +108,7 @@ __device__ __forceinline__ R conv_x(R u, bool nearb, R fm2, R fm1, R f0, R fp1, 
     R sgn = u > R(-1) ? R(1) : R(-1);  // sign(1, ceiling(u))
     R Pe = sgn * c.tf * u * c.dx;
     if (nearb) return u * (fp1 - fm1) * c.inv2dx;
-    if (Pe > R(2) && Pe < R(50)) {
+    if (pe_window(Pe, R(50), c.pe_mode)) {
         R t1 = abs(u) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25x;
         R t2 = u * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12x;
         return t1 + t2;
@@ -103,10 +123,11 @@ __device__ __forceinline__ R conv_y(R v, bool nearb, R fm2, R fm1, R f0, R fp1, 
     R sgn = v > R(-1) ? R(1) : R(-1);
     R Pe = sgn * c.tf * v * c.dy;
     if (nearb) {
+        if (c.ycen) return v * (fp1 - fm1) * c.h05y;
         R a1 = max(v, R(0)), b = min(v, R(0));
         return a1 * ((f0 - fm1) * c.invdy) + b * ((fp1 - f0) * c.invdy);
     }
-    if (Pe > R(2) && Pe < R(50)) {
+    if (pe_window(Pe, R(50), c.pe_mode)) {
         R t1 = abs(v) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25y;
         R t2 = v * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12y;
         return t1 + t2;
@@ -121,7 +142,7 @@ __device__ __forceinline__ R conv_z(R w, R dz, bool nearb, R fm2, R fm1, R f0, R
     R sgn = w > R(-1) ? R(1) : R(-1);
     R Pe = (sgn * c.tf * w * dz);
     if (nearb) return (w * (fp1 - fm1) * c.h05z);
-    if (Pe > R(2) && Pe < R(5)) {
+    if (pe_window(Pe, R(5), c.pe_mode)) {
         R t1 = abs(w) * (fp2 - R(4) * fp1 + R(6) * f0 - R(4) * fm1 + fm2) * c.q25z;
         R t2 = w * (-fp2 + R(8) * fp1 - R(8) * fm1 + fm2) * c.c12z;
         return t1 + t2;
@@ -601,13 +622,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_div_diag(Geom g, double invdx, 
 // -------------------------- per-step fluctuations, KE, blowup (:1707-1775)
 // Ufluc = U - means on every slab's planes; only the recycling plane irec is
 // kept (ufl_live); KE sum -> red[slot]; max fluctuation -> red[slot+1].
+// Columns i_lo..i_hi (0-based): all, or 1..nx-2 for dnssetbl
+// (dnssetbl.f90:1228-1236).
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const T* __restrict__ U1,
                                                          const T* __restrict__ U2, const T* __restrict__ U3,
                                                          const double* __restrict__ usum2,
                                                          const double* __restrict__ vsum2,
                                                          const double* __restrict__ wsum2, double* __restrict__ ufl_live,
-                                                         int irec0, RedWork rw, DevScalars* sc, int slot) {
+                                                         int irec0, RedWork rw, DevScalars* sc, int slot, int i_lo,
+                                                         int i_hi) {
     __shared__ double s_red[RED_THREADS / 32];
     const int nx = g.nx, J = g.ny - 2, nk = g.nz - 2;
     const long long n = (long long)nx * J * nk;
@@ -616,6 +640,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_fluc_ke(Geom g, const T* __rest
     for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < n;
          t0 += (long long)gridDim.x * blockDim.x) {
         int i = (int)(t0 % nx);
+        if (i < i_lo || i > i_hi) continue;
         long long r = t0 / nx;
         int j = 1 + (int)(r % J);
         int k = 1 + (int)(r / J);
@@ -735,16 +760,18 @@ __global__ void k_rescale(Geom g, int irec0, double cum, double ue, double re, c
     }
 }
 
-// refresh Ufluc(irec,:,k,:) with the new means and zero the sums (:2341-2365)
+// refresh Ufluc(irec,:,k,:) with the new means on planes k_lo..k_hi
+// (0-based; every slab's, :2341-2349, or rank 0's for dnssetbl,
+// dnssetbl.f90:1033-1041) and zero the sums (:2351-2365)
 template <typename T>
 __global__ void k_rescale_tail(Geom g, int irec0, const T* __restrict__ U1, const T* __restrict__ U2,
                                const T* __restrict__ U3, const double* __restrict__ usum2,
                                const double* __restrict__ vsum2, const double* __restrict__ wsum2,
-                               double* __restrict__ ufl_live, double* __restrict__ sums) {
+                               double* __restrict__ ufl_live, double* __restrict__ sums, int k_lo, int k_hi) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = g.ny - 2;
     const size_t n2 = (size_t)g.nx * g.nz;
-    if (t < J * (g.nz - 2)) {
+    if (t < J * (g.nz - 2) && 1 + t / J >= k_lo && 1 + t / J <= k_hi) {
         int j = 1 + t % J, k = 1 + t / J;
         long long p = idx(g, irec0, j, k);
         size_t q = (size_t)irec0 + (size_t)g.nx * k, pl = (size_t)g.ny * g.nz, pj = (size_t)j + (size_t)g.ny * k;
@@ -775,16 +802,22 @@ int launch_save_uold(tbl_handle* h) {
 int launch_inflow(tbl_handle* h) {
     const Geom& g = h->g;
     int n = (g.ny - 2) * (g.nz - 2);
+    const int var = h->cfg.variant;
+    // eps = min(cnt2 * 5e-5, 1) (fnldnstbl.f90:561-565), min(nstep * 5e-5, 1) (dnssetbl.f90:259-262)
+    double eps = (var == TBL_VARIANT_ORIGINAL ? (double)h->cnt2 : (double)h->nstep) * (5.0e-5);
+    if (eps > 1.0) eps = 1.0;
+    const int ramp = var != TBL_VARIANT_DNSTBL2, vlam = var == TBL_VARIANT_DNSSETBL;
+    const int wcol = var == TBL_VARIANT_DNSSETBL ? 0 : g.nx - 2;
     if (mixed(h))
         k_inflow<float><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2, h->vsum2,
                                                                  h->wsum2, h->wt, h->ume1, h->newk, h->ufl_file,
                                                                  h->ufl_live, h->slab_of_k, h->slabs, h->sc,
-                                                                 h->cfg.irec - 1, h->cfg.ue);
+                                                                 h->cfg.irec - 1, h->cfg.ue, ramp, eps, vlam, wcol);
     else
         k_inflow<double><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2,
                                                                   h->wsum2, h->wt, h->ume1, h->newk, h->ufl_file,
                                                                   h->ufl_live, h->slab_of_k, h->slabs, h->sc,
-                                                                  h->cfg.irec - 1, h->cfg.ue);
+                                                                  h->cfg.irec - 1, h->cfg.ue, ramp, eps, vlam, wcol);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -799,7 +832,10 @@ static ConvCoef<R> conv_coef(const tbl_config& c) {
     cc.c12x = (R)(c12 * invdx); cc.c12y = (R)(c12 * invdy); cc.c12z = (R)(c12 * invdxi);
     cc.q25x = (R)(0.25 * invdx); cc.q25y = (R)(0.25 * invdy); cc.q25z = (R)(0.25 * invdxi);
     cc.h05z = (R)(0.5 * invdxi);
+    cc.h05y = (R)(0.5 * invdy);
     cc.dt = (R)c.dt;
+    cc.pe_mode = c.variant == TBL_VARIANT_DNSSETBL ? 2 : (c.variant == TBL_VARIANT_ORIGINAL ? 1 : 0);
+    cc.ycen = c.variant == TBL_VARIANT_DNSSETBL ? 1 : 0;
     return cc;
 }
 
@@ -939,19 +975,21 @@ int launch_project_bcs(tbl_handle* h) {
 // Mass flux through the five cross-stream planes i = 5, 20, 40, 60, 85
 // (1-based, :95; clamped to nx-1) (:1578-1594): cell averages of u times the
 // cell area dy (x3(k+1) - x3(k)) over the span and the whole height, divided
-// by the area Av.  One block per plane.
+// by the area Av.  One block per plane.  k_lo = 1 starts at the second cell
+// layer: dnssetbl sums each slab's own planes, so the wall layer drops out
+// (dnssetbl.f90:887-893).
 template <typename T>
 __global__ void __launch_bounds__(256) k_mass_flux(Geom g, double dy, double Av, const double* __restrict__ x3,
-                                                   const T* __restrict__ U1, double* __restrict__ ub) {
+                                                   const T* __restrict__ U1, double* __restrict__ ub, int k_lo) {
     __shared__ double s_red[256 / 32];
     const int planes[5] = {5, 20, 40, 60, 85};
     const int q = blockIdx.x;
     const int ip = (planes[q] < g.nx - 1 ? planes[q] : g.nx - 1) - 1;  // 0-based
     const int J = g.ny - 2;
-    const int ncell = J * (g.nz - 1);
+    const int ncell = J * (g.nz - 1 - k_lo);
     double acc = 0.0;
     for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-        const int j = 1 + t % J, k = t / J;
+        const int j = 1 + t % J, k = k_lo + t / J;
         const int jp = j == g.ny - 2 ? 1 : j + 1;
         const double dAv = dy * (x3[k + 1] - x3[k]);
         acc += (0.25 * ((double)U1[idx(g, ip, j, k)] + (double)U1[idx(g, ip, jp, k)] +
@@ -965,14 +1003,14 @@ __global__ void __launch_bounds__(256) k_mass_flux(Geom g, double dy, double Av,
 // Wall shear (:1616-1681): for every interior column the span sum of
 // (dw/dx + du/dz)/Re at the wall -- dw/dx 6th-order central, 2nd order within
 // three points of the ends; du/dz one-sided 2nd order on the stretched grid --
-// added to the accumulator sumxz; at a window end (every 500 steps) the
-// window mean sumxz/500 is kept and the accumulator restarts.  One block per
-// column.
+// added to the accumulator sumxz; at a window end (every `win` steps: 500,
+// originalTBL 1000, fnldnstbl.f90:1679-1681) the window mean sumxz/win is
+// kept and the accumulator restarts.  One block per column.
 template <typename T>
 __global__ void __launch_bounds__(128) k_wall_shear(Geom g, double dx, double re, double d1, double d2,
                                                     const T* __restrict__ U1, const T* __restrict__ U3,
                                                     double* __restrict__ sumxz, double* __restrict__ window,
-                                                    int close_window) {
+                                                    int close_window, double win) {
     __shared__ double s_red[128 / 32];
     const int i = 1 + blockIdx.x;  // 0-based interior column
     const int nx = g.nx;
@@ -994,7 +1032,7 @@ __global__ void __launch_bounds__(128) k_wall_shear(Geom g, double dx, double re
     if (threadIdx.x == 0) {
         const double s = acc + sumxz[i];
         if (close_window) {
-            window[i] = s / 500.0;
+            window[i] = s / win;
             sumxz[i] = 0.0;
         } else {
             sumxz[i] = s;
@@ -1005,16 +1043,18 @@ __global__ void __launch_bounds__(128) k_wall_shear(Geom g, double dx, double re
 int launch_flux_shear(tbl_handle* h) {
     const Geom& g = h->g;
     const double d1 = h->x3h[1] - h->x3h[0], d2 = h->x3h[2] - h->x3h[0];
-    const int close = (h->nstep % 500 == 0) ? 1 : 0;
+    const int win = h->cfg.variant == TBL_VARIANT_ORIGINAL ? 1000 : 500;
+    const int close = (h->nstep % win == 0) ? 1 : 0;
+    const int k_lo = h->cfg.variant == TBL_VARIANT_DNSSETBL ? 1 : 0;
     if (close) TBL_CUDA_TRY(cudaMemsetAsync(h->tauw_win, 0, (size_t)g.nx * 8, h->stream));
     if (mixed(h)) {
-        k_mass_flux<float><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->Uf[0], h->ubulk);
+        k_mass_flux<float><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->Uf[0], h->ubulk, k_lo);
         k_wall_shear<float><<<g.nx - 2, 128, 0, h->stream>>>(g, h->cfg.dx, h->cfg.re, d1, d2, h->Uf[0], h->Uf[2],
-                                                             h->sumxz, h->tauw_win, close);
+                                                             h->sumxz, h->tauw_win, close, (double)win);
     } else {
-        k_mass_flux<double><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->U[0], h->ubulk);
+        k_mass_flux<double><<<5, 256, 0, h->stream>>>(g, h->cfg.dy, h->area_mf, h->x3, h->U[0], h->ubulk, k_lo);
         k_wall_shear<double><<<g.nx - 2, 128, 0, h->stream>>>(g, h->cfg.dx, h->cfg.re, d1, d2, h->U[0], h->U[2],
-                                                              h->sumxz, h->tauw_win, close);
+                                                              h->sumxz, h->tauw_win, close, (double)win);
     }
     h->launches += 2;
     return TBL_OK;
@@ -1036,15 +1076,17 @@ int launch_div_diag(tbl_handle* h, int nblocks, int slot) {
 
 int launch_fluc_ke(tbl_handle* h, int nblocks, int slot) {
     const Geom& g = h->g;
+    const bool sete = h->cfg.variant == TBL_VARIANT_DNSSETBL;
+    const int i_lo = sete ? 1 : 0, i_hi = sete ? g.nx - 2 : g.nx - 1;
     TBL_CUDA_TRY(cudaMemsetAsync(&h->sc->red[slot + 1], 0, sizeof(double), h->stream));
     if (mixed(h))
         k_fluc_ke<float><<<nblocks, RED_THREADS, 0, h->stream>>>(g, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2,
                                                                  h->vsum2, h->wsum2, h->ufl_live, h->cfg.irec - 1,
-                                                                 h->red, h->sc, slot);
+                                                                 h->red, h->sc, slot, i_lo, i_hi);
     else
         k_fluc_ke<double><<<nblocks, RED_THREADS, 0, h->stream>>>(g, h->U[0], h->U[1], h->U[2], h->usum2, h->vsum2,
                                                                   h->wsum2, h->ufl_live, h->cfg.irec - 1, h->red,
-                                                                  h->sc, slot);
+                                                                  h->sc, slot, i_lo, i_hi);
     LAUNCH_COUNT(h);
     return TBL_OK;
 }
@@ -1053,10 +1095,10 @@ int launch_stats(tbl_handle* h) {
     const Geom& g = h->g;
     int n = g.nx * g.nz;
     if (mixed(h))
-        k_stats<float><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->cfg.dy, h->stats_A, h->Uf[0], h->Uf[1],
+        k_stats<float><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->stats_dA, h->stats_A, h->Uf[0], h->Uf[1],
                                                                h->Uf[2], h->sums);
     else
-        k_stats<double><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->cfg.dy, h->stats_A, h->U[0], h->U[1], h->U[2],
+        k_stats<double><<<(n + 127) / 128, 128, 0, h->stream>>>(g, h->stats_dA, h->stats_A, h->U[0], h->U[1], h->U[2],
                                                                 h->sums);
     LAUNCH_COUNT(h);
     return TBL_OK;
@@ -1069,12 +1111,14 @@ int launch_rescale(tbl_handle* h) {
     int n = (g.ny - 2) * (g.nz - 2);
     int nb = (n + 255) / 256;
     if (nb < 64) nb = 64;
+    const bool sete = h->cfg.variant == TBL_VARIANT_DNSSETBL;
+    const int k_lo = sete ? h->bn[0] : 1, k_hi = sete ? h->en[0] : g.nz - 2;
     if (mixed(h))
         k_rescale_tail<float><<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->Uf[0], h->Uf[1], h->Uf[2], h->usum2,
-                                                         h->vsum2, h->wsum2, h->ufl_live, h->sums);
+                                                         h->vsum2, h->wsum2, h->ufl_live, h->sums, k_lo, k_hi);
     else
         k_rescale_tail<double><<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->U[0], h->U[1], h->U[2], h->usum2,
-                                                          h->vsum2, h->wsum2, h->ufl_live, h->sums);
+                                                          h->vsum2, h->wsum2, h->ufl_live, h->sums, k_lo, k_hi);
     h->launches += 2;
     return TBL_OK;
 }
