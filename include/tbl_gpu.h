@@ -256,6 +256,8 @@ int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches
  * more than TBL_NOALLOC_MAX_POINTS interior points are rejected with
  * TBL_ERR_TOO_LARGE. */
 #define TBL_ERR_TOO_LARGE     -10
+/* A restart or counter file could not be opened, read, parsed or written. */
+#define TBL_ERR_IO            -11
 #define TBL_NOALLOC_BLOCKS     4096
 #define TBL_NOALLOC_MAX_POINTS ((int64_t)TBL_NOALLOC_BLOCKS * 256 * 64)
 int tbl_div_diag_noalloc(const tbl_config* cfg, const double* jacinv, const double* u, const double* v,
@@ -340,6 +342,46 @@ const char* tbl_status_string(int status);
 
 /* Number of kernel launches issued by this handle so far (instrumentation). */
 int64_t tbl_launch_count(tbl_handle* h);
+
+/* ------------------------------------------------------------ restart files
+ * Host-only readers and writers of the reference's restart files (no device,
+ * no handle): Tecplot ASCII POINT, i outermost, then j, then k.  Arrays are
+ * those of tbl_state / tbl_mesh (Fortran order, nx*ny*nz and nx*nz); ranges
+ * are 1-based and inclusive.  The state's time and nstep go to the title.
+ * Values are written with 15 significant digits (E22.15), as the reference
+ * writes them. */
+#define TBL_TP_DNSTBL2   0  /* 15 columns x y z U V W P Um Vm Wm Uf Vf Wf Wt Nk (dnstbl2/dnstbl.f90:2357-2384) */
+#define TBL_TP_ORIGINAL  1  /* 8 columns x y z U V W T P, T written as 0 (originalTBL/fnldnstbl.f90:1696-1717) */
+#define TBL_TP_DNSSETBL  2  /* 7 columns x y z U V W P (dnssetbl/dnssetbl.f90:908-932) */
+
+/* One file of points i = 1..nx, j = j0..j1, k = k0..k1.  header: 0 none (the
+ * files of ranks > 0), 1 the program's own writer (dnssetbl's title also
+ * carries nproc), 2 the merger's.  Replaces the WRITE loops at
+ * dnstbl2/dnstbl.f90:2357-2377. */
+int tbl_tp_write(const char* path, int32_t format, const tbl_mesh* mesh, const tbl_state* st, int32_t nx,
+                 int32_t ny, int32_t nz, int32_t j0, int32_t j1, int32_t k0, int32_t k1, int32_t header,
+                 int32_t nproc);
+/* The per-rank files dir/3D%03d.tp (dir/3D%03d.dat for dnssetbl) of an
+ * nproc-rank run: j = 2..ny-1 and the rank's k range (dnstbl2/dnstbl.f90:
+ * 469-485, 2357-2377; dnssetbl/dnssetbl.f90:78-92, 908-932). */
+int tbl_tp_write_ranks(const char* dir, int32_t format, const tbl_mesh* mesh, const tbl_state* st, int32_t nx,
+                       int32_t ny, int32_t nz, int32_t nproc);
+/* Merge the per-rank files in dir into out_path with every j (the periodic
+ * ghost rows filled), as dnstbl/restart.f90:17-86, originalTBL/restart.f90
+ * and dnssetbl/combineFile.f90 do. */
+int tbl_tp_merge(const char* dir, int32_t format, int32_t nz, int32_t nproc, const char* out_path);
+/* Read a merged file (every j) into st (any array pointer may be NULL to
+ * skip it) and x1/x2/x3 (may be NULL); sets st->time and st->nstep
+ * (dnstbl2/dnstbl.f90:147-159, 350-358).  The file's zone must be nx, ny, nz. */
+int tbl_tp_read(const char* path, int32_t format, int32_t nx, int32_t ny, int32_t nz, double* x1, double* x2,
+                double* x3, tbl_state* st);
+/* The counter files dir/cnt ("nz cnt proc") and dir/cnt2 (:147-153, :2054-2056, :2349-2352). */
+int tbl_counters_write(const char* dir, int32_t nz, int32_t cnt, int32_t nproc, int32_t cnt2);
+int tbl_counters_read(const char* dir, int32_t* nz, int32_t* cnt, int32_t* nproc, int32_t* cnt2);
+/* dnssetbl's statData.dat: usum2, vsum2, wsum2 at plane irec, Wt(1,k), new(k)
+ * per k, FORMAT(4(1X,F15.7),I5.3) (dnssetbl/dnssetbl.f90:1203-1208, 136-140). */
+int tbl_statdata_write(const char* path, int32_t nx, int32_t nz, int32_t irec, const tbl_state* st);
+int tbl_statdata_read(const char* path, int32_t nx, int32_t nz, int32_t irec, tbl_state* st);
 
 #ifdef __cplusplus
 }

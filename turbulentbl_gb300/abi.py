@@ -18,6 +18,7 @@ TBL_ERR_NO_DEVICE = -7
 TBL_ERR_REPLAY = -8
 TBL_ERR_ZERO_RHS = -9
 TBL_ERR_TOO_LARGE = -10
+TBL_ERR_IO = -11
 
 STATUS_NAMES = {
     TBL_OK: "OK",
@@ -31,7 +32,12 @@ STATUS_NAMES = {
     TBL_ERR_REPLAY: "REPLAY",
     TBL_ERR_ZERO_RHS: "ZERO_RHS",
     TBL_ERR_TOO_LARGE: "TOO_LARGE",
+    TBL_ERR_IO: "IO",
 }
+
+TBL_TP_DNSTBL2 = 0
+TBL_TP_ORIGINAL = 1
+TBL_TP_DNSSETBL = 2
 
 TBL_PREC_FP64 = 0
 TBL_PREC_MIXED = 1

@@ -962,6 +962,7 @@ const char* tbl_status_string(int status) {
         case TBL_ERR_REPLAY: return "replay counts exhausted";
         case TBL_ERR_ZERO_RHS: return "zero PPE residual at the first restart";
         case TBL_ERR_TOO_LARGE: return "grid larger than the fixed scratch of the allocation-free entry point";
+        case TBL_ERR_IO: return "restart or counter file could not be opened, read, parsed or written";
         default: return "unknown status";
     }
 }

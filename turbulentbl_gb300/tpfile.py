@@ -1,183 +1,159 @@
-"""The reference's restart and counter files (host side).
+"""The reference's restart and counter files, through the library's C ABI.
 
-Formats (theparvezahmad/turbulentBL):
-  * `3D.tp` / `3D%03d.tp`, Tecplot ASCII POINT data with 15 columns per point
-    x, y, z, U, V, W, P, Um, Vm, Wm, Uf, Vf, Wf, Wt, Nk written with
-    FORMAT(3(1X,F10.6),11(1X,E22.15),(1X,I4)) (dnstbl2/dnstbl.f90:2380-2397,
-    format 97), an empty record before every i and every j block, and the
-    header records 03/04 (title with time and nstep, variables, zone sizes).
-  * the merged `3D.tp` that dnstbl2 reads (:147-159, :350-358) has all j
-    (ghost rows included, dnstbl/restart.f90:67-86); a per-rank file holds
-    j = 2..ny-1 and k = istart..iend of that rank (:2387-2396).
-  * `cnt` holds "nz cnt proc" (list-directed), `cnt2` holds "cnt2".
+The readers and writers are the C++ ones in libtblgpu.so
+(csrc/tbl_restart.cpp: tbl_tp_write, tbl_tp_write_ranks, tbl_tp_merge,
+tbl_tp_read, tbl_counters_*, tbl_statdata_*); they touch no device.  Formats
+(``fmt``): 0 dnstbl2's 15 columns (x y z U V W P Um Vm Wm Uf Vf Wf Wt Nk),
+1 originalTBL's 8 (x y z U V W T P), 2 dnssetbl's 7 (x y z U V W P).
 
-Values round-trip at 15 significant digits (E22.15), as in the reference, so a
-restart is not bit-exact in FP64.
+Values carry 15 significant digits (E22.15), as the reference writes them,
+so a restart through these files is not bit-exact in FP64.
 """
+import ctypes as C
 import os
 
 import numpy as np
 
-COLS = ["x", "y", "z", "u", "v", "w", "p", "usum2", "vsum2", "wsum2", "uf", "vf", "wf", "wt", "newk"]
+from . import abi
+from .runner import TblError
+
+_declared = False
 
 
-def fortran_e(v, w=22, d=15):
-    """Fortran Ew.d: 0.ddd...E+xx with d digits after the point."""
-    if v == 0.0 or not np.isfinite(v):
-        if not np.isfinite(v):
-            return ("NaN" if np.isnan(v) else ("Infinity" if v > 0 else "-Infinity")).rjust(w)
-        m, e = 0.0, 0
-    else:
-        e = int(np.floor(np.log10(abs(v)))) + 1
-        m = abs(v) / 10.0 ** e
-        # rounding can carry into the next decade
-        if round(m, d) >= 1.0:
-            e += 1
-            m = abs(v) / 10.0 ** e
-    digits = f"{m:.{d}f}"
-    if digits.startswith("1."):  # carry after rounding
-        e += 1
-        digits = f"{abs(v) / 10.0 ** e:.{d}f}"
-    sign = "-" if v < 0 else ""
-    es = f"E{'+' if e >= 0 else '-'}{abs(e):02d}"
-    return (sign + digits + es).rjust(w)
+def _lib():
+    global _declared
+    from .lib import load
+    lib = load()
+    if not _declared:
+        I, P, S = C.c_int32, C.c_void_p, C.c_char_p
+        Mp, Sp = C.POINTER(abi.TblMesh), C.POINTER(abi.TblState)
+        ip = C.POINTER(C.c_int32)
+        dp = C.POINTER(C.c_double)
+        sigs = {
+            "tbl_tp_write": [S, I, Mp, Sp, I, I, I, I, I, I, I, I, I],
+            "tbl_tp_write_ranks": [S, I, Mp, Sp, I, I, I, I],
+            "tbl_tp_merge": [S, I, I, I, S],
+            "tbl_tp_read": [S, I, I, I, I, dp, dp, dp, Sp],
+            "tbl_counters_write": [S, I, I, I, I],
+            "tbl_counters_read": [S, ip, ip, ip, ip],
+            "tbl_statdata_write": [S, I, I, I, Sp],
+            "tbl_statdata_read": [S, I, I, I, Sp],
+        }
+        for name, args in sigs.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        _declared = True
+    return lib
 
 
-def _row(x1, x2, x3, vals, nk):
-    s = " " + f"{x1:10.6f}" + " " + f"{x2:10.6f}" + " " + f"{x3:10.6f}"
-    for v in vals:
-        s += " " + fortran_e(float(v))
-    s += " " + f"{int(nk):4d}"
-    return s + "\n"
+def _check(st, what):
+    if st != abi.TBL_OK:
+        raise TblError(st, what)
 
 
-def write_tp(path, mesh, st, time, nstep, j_range=None, k_range=None, header=True, ny_header=None):
-    """Write a 3D.tp-format file.  j_range/k_range are 0-based inclusive
-    ranges (default: all j, all k, the merged file)."""
-    nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
-    j0, j1 = j_range if j_range is not None else (0, ny - 1)
-    k0, k1 = k_range if k_range is not None else (0, nz - 1)
-    arrs = [st[c] for c in ("u", "v", "w", "p")]
-    two = [st[c] for c in ("usum2", "vsum2", "wsum2")]
-    fl = [st.get(c) for c in ("uf", "vf", "wf")]
-    wt, newk = st["wt"], st["newk"]
-    with open(path, "w") as f:
-        if header:
-            f.write(f'TITLE ="{time:20.10f}{nstep:9d}"\n')
-            f.write(' Variables = "x","y","z","U","V","W","P","Um","Vm","Wm","Uf","Vf","Wf","Wt","Nk"\n')
-            f.write(f"ZONE k={nx:4d},j={(ny_header if ny_header is not None else j1 - j0 + 1):4d},"
-                    f"i={nz:4d},DATAPACKING=\"POINT\"\n")
-        for i in range(nx):
-            f.write("\n")
-            for j in range(j0, j1 + 1):
-                f.write("\n")
-                for k in range(k0, k1 + 1):
-                    vals = [a[i, j, k] for a in arrs] + [a[i, k] for a in two] + \
-                           [(a[i, j, k] if a is not None else 0.0) for a in fl] + [wt[i, k]]
-                    f.write(_row(mesh.x1[i], mesh.x2[j], mesh.x3[k], vals, newk[k]))
+def _mesh_struct(mesh):
+    m = abi.TblMesh()
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (mesh.x1, mesh.x2, mesh.x3)]
+    m.x1, m.x2, m.x3 = (abi.dptr(a) for a in keep)
+    return m, keep
 
 
-def read_tp(path, nx=None, ny=None, nz=None):
-    """Read a merged 3D.tp (all j).  Returns (state dict, time, nstep)."""
-    with open(path) as f:
-        title = f.readline()
-        f.readline()
-        zone = f.readline()
-        body = f.read().split()
-    t = title.split('"')[1]
-    time = float(t[:20])
-    nstep = int(t[20:29])
-    z = zone.replace(",", " ").replace("=", " ").split()
-    znx, zny, znz = int(z[z.index("k") + 1]), int(z[z.index("j") + 1]), int(z[z.index("i") + 1])
-    nx, ny, nz = nx or znx, ny or zny, nz or znz
-    a = np.array(body, dtype=object).reshape(nx, ny, nz, 15)
-    num = a[..., :14].astype(np.float64)
-    newk = a[0, 0, :, 14].astype(np.int64).astype(np.int32)
-    st = {}
-    for q, c in enumerate(("u", "v", "w", "p")):
-        st[c] = np.asfortranarray(num[..., 3 + q])
-    for q, c in enumerate(("usum2", "vsum2", "wsum2")):
-        st[c] = np.asfortranarray(num[:, 0, :, 7 + q])
-    for q, c in enumerate(("uf", "vf", "wf")):
-        st[c] = np.asfortranarray(num[..., 10 + q])
-    st["wt"] = np.asfortranarray(num[:, 0, :, 13])
-    st["newk"] = newk
-    st["x1"], st["x2"], st["x3"] = num[:, 0, 0, 0], num[0, :, 0, 1], num[0, 0, :, 2]
-    return st, time, nstep
+def _state_struct(st, time, nstep):
+    s = abi.TblState()
+    keep = []
+    for name in ("u", "v", "w", "p", "uf", "vf", "wf"):
+        if st.get(name) is not None:
+            a = np.asfortranarray(st[name], dtype=np.float64)
+            keep.append(a)
+            setattr(s, name, abi.dptr(a))
+    for name in ("usum2", "vsum2", "wsum2", "wt"):
+        if st.get(name) is not None:
+            a = np.asfortranarray(st[name], dtype=np.float64)
+            keep.append(a)
+            setattr(s, name, abi.dptr(a))
+    if st.get("newk") is not None:
+        nk = np.ascontiguousarray(st["newk"], dtype=np.int32)
+        keep.append(nk)
+        s.newk = abi.iptr(nk)
+    s.time, s.nstep = float(time), int(nstep)
+    return s, keep
 
 
-def rank_ranges(nz, nproc):
-    """istart..iend (0-based inclusive) of each rank's restart file (:469-485)."""
-    loc = (nz - 1) // nproc
-    out = []
-    for r in range(nproc):
-        bn = 1 + r * loc
-        en = bn + loc - 1 if r < nproc - 1 else nz - 2
-        ist = bn - 1 if r == 0 else bn
-        ien = en + 1 if r == nproc - 1 else en
-        out.append((ist, ien))
-    return out
+def _b(path):
+    return os.fsencode(str(path))
 
 
-def write_rank_files(dirname, mesh, st, time, nstep, nproc):
-    """The per-rank restart files 3D%03d.tp (j = 2..ny-1, own k range)."""
-    for r, (k0, k1) in enumerate(rank_ranges(mesh.nz, nproc)):
-        write_tp(os.path.join(dirname, f"3D{r + 1:03d}.tp"), mesh, st, time, nstep,
-                 j_range=(1, mesh.ny - 2), k_range=(k0, k1), header=(r == 0), ny_header=mesh.ny - 2)
+def write_tp(path, mesh, st, time, nstep, j_range=None, k_range=None, header=1, fmt=0, nproc=0):
+    """One file of points i = all, j in j_range, k in k_range (0-based
+    inclusive; default every j and k).  header: 0 none, 1 the program's own
+    writer, 2 the merger's."""
+    j0, j1 = j_range if j_range is not None else (0, mesh.ny - 1)
+    k0, k1 = k_range if k_range is not None else (0, mesh.nz - 1)
+    m, km = _mesh_struct(mesh)
+    s, ks = _state_struct(st, time, nstep)
+    _check(_lib().tbl_tp_write(_b(path), fmt, C.byref(m), C.byref(s), mesh.nx, mesh.ny, mesh.nz, j0 + 1, j1 + 1,
+                               k0 + 1, k1 + 1, header, nproc), "tbl_tp_write")
 
 
-def merge_rank_files(dirname, nz, nproc, out_name="3D.tp"):
-    """The restart merger (dnstbl/restart.f90:17-86): concatenate the ranks'
-    k ranges, add the periodic ghost rows j=1, ny for U, V, W (P and the
-    fluctuation columns of the ghost rows are written as zero, as the merger
-    leaves them unset), and write the merged file with x2(ny) rewritten."""
-    with open(os.path.join(dirname, "3D001.tp")) as f:
-        title = f.readline()
-        f.readline()
-        zone = f.readline()
-    z = zone.replace(",", " ").replace("=", " ").split()
-    nx, nyi = int(z[z.index("k") + 1]), int(z[z.index("j") + 1])
-    ny = nyi + 2
-    data = np.zeros((nx, ny, nz, 15))
-    for r, (k0, k1) in enumerate(rank_ranges(nz, nproc)):
-        with open(os.path.join(dirname, f"3D{r + 1:03d}.tp")) as f:
-            if r == 0:
-                for _ in range(3):
-                    f.readline()
-            vals = np.array(f.read().split(), dtype=np.float64)
-        data[:, 1:ny - 1, k0:k1 + 1, :] = vals.reshape(nx, nyi, k1 - k0 + 1, 15)
-    for q in (3, 4, 5):
-        data[:, 0, :, q] = data[:, ny - 2, :, q]
-        data[:, ny - 1, :, q] = data[:, 1, :, q]
-    for q in (0, 2, 7, 8, 9, 13, 14):
-        data[:, 0, :, q] = data[:, 1, :, q]
-        data[:, ny - 1, :, q] = data[:, 1, :, q]
-    dy = data[0, 2, 0, 1] - data[0, 1, 0, 1]
-    data[:, 0, :, 1] = 0.0
-    data[:, ny - 1, :, 1] = data[0, 1, 0, 1] + (ny - 2) * dy
-    with open(os.path.join(dirname, out_name), "w") as f:
-        f.write(title)
-        f.write(' Variables = "x","y","z","U","V","W","P","Um","Vm","Wm","Uf","Vf","Wf","Wt","Nk"\n')
-        f.write(f"ZONE k={nx:4d},j={ny:4d},i={nz:4d},DATAPACKING=\"POINT\"\n")
-        for i in range(nx):
-            f.write("\n")
-            for j in range(ny):
-                f.write("\n")
-                for k in range(nz):
-                    d = data[i, j, k]
-                    f.write(_row(d[0], d[1], d[2], d[3:14], d[14]))
+def write_rank_files(dirname, mesh, st, time, nstep, nproc, fmt=0):
+    """The per-rank files 3D%03d.tp (3D%03d.dat for dnssetbl): j = 2..ny-1 and
+    each rank's k range."""
+    m, km = _mesh_struct(mesh)
+    s, ks = _state_struct(st, time, nstep)
+    _check(_lib().tbl_tp_write_ranks(_b(dirname), fmt, C.byref(m), C.byref(s), mesh.nx, mesh.ny, mesh.nz, nproc),
+           "tbl_tp_write_ranks")
+
+
+def merge_rank_files(dirname, nz, nproc, out_name="3D.tp", fmt=0):
+    """Merge the per-rank files into one with every j (the restart mergers)."""
+    _check(_lib().tbl_tp_merge(_b(dirname), fmt, nz, nproc, _b(os.path.join(str(dirname), out_name))),
+           "tbl_tp_merge")
+
+
+def read_tp(path, nx, ny, nz, fmt=0):
+    """Read a merged file.  Returns (state dict, time, nstep); the state has
+    x1, x2, x3, u, v, w, p and, for the 15-column format, the recycling and
+    statistics columns."""
+    out = {"x1": np.zeros(nx), "x2": np.zeros(ny), "x3": np.zeros(nz)}
+    names = ["u", "v", "w", "p"] + (["uf", "vf", "wf"] if fmt == 0 else [])
+    for n in names:
+        out[n] = np.zeros((nx, ny, nz), order="F")
+    if fmt == 0:
+        for n in ("usum2", "vsum2", "wsum2", "wt"):
+            out[n] = np.zeros((nx, nz), order="F")
+        out["newk"] = np.zeros(nz, dtype=np.int32)
+    s, _ = _state_struct(out, 0.0, 0)
+    _check(_lib().tbl_tp_read(_b(path), fmt, nx, ny, nz, abi.dptr(out["x1"]), abi.dptr(out["x2"]),
+                              abi.dptr(out["x3"]), C.byref(s)), "tbl_tp_read")
+    return out, s.time, s.nstep
 
 
 def write_counters(dirname, nz, cnt, nproc, cnt2):
-    with open(os.path.join(dirname, "cnt"), "w") as f:
-        f.write(f"{nz:12d}{cnt:12d}{nproc:12d}\n")
-    with open(os.path.join(dirname, "cnt2"), "w") as f:
-        f.write(f"{cnt2:12d}\n")
+    _check(_lib().tbl_counters_write(_b(dirname), nz, cnt, nproc, cnt2), "tbl_counters_write")
 
 
 def read_counters(dirname):
-    with open(os.path.join(dirname, "cnt")) as f:
-        nz, cnt, nproc = (int(x) for x in f.read().split()[:3])
-    with open(os.path.join(dirname, "cnt2")) as f:
-        cnt2 = int(f.read().split()[0])
-    return nz, cnt, nproc, cnt2
+    v = [C.c_int32() for _ in range(4)]
+    _check(_lib().tbl_counters_read(_b(dirname), *[C.byref(x) for x in v]), "tbl_counters_read")
+    return tuple(int(x.value) for x in v)
+
+
+def write_statdata(path, st, irec):
+    """dnssetbl's statData.dat: the recycling means at irec, Wt(1,k), new(k)."""
+    nx, nz = st["usum2"].shape
+    s, ks = _state_struct(st, 0.0, 0)
+    _check(_lib().tbl_statdata_write(_b(path), nx, nz, irec, C.byref(s)), "tbl_statdata_write")
+
+
+def read_statdata(path, st, irec):
+    """Fill st's usum2/vsum2/wsum2 at irec, wt(1,:) and newk from statData.dat
+    (st's arrays are updated in place; they must be float64 Fortran arrays)."""
+    nx, nz = st["usum2"].shape
+    for n in ("usum2", "vsum2", "wsum2", "wt"):
+        assert st[n].dtype == np.float64 and st[n].flags.f_contiguous
+    assert st["newk"].dtype == np.int32
+    s = abi.TblState()
+    s.usum2, s.vsum2, s.wsum2, s.wt = (abi.dptr(st[n]) for n in ("usum2", "vsum2", "wsum2", "wt"))
+    s.newk = abi.iptr(st["newk"])
+    _check(_lib().tbl_statdata_read(_b(path), nx, nz, irec, C.byref(s)), "tbl_statdata_read")
