@@ -25,6 +25,7 @@ namespace tbl {
 
 void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
 
+constexpr int CHUNK = 4;          // i-points per lane per wavefront step
 constexpr int KG = 4;             // k-planes (warps) per wavefront CTA
 constexpr int RED_THREADS = 256;  // threads per reduction block
 

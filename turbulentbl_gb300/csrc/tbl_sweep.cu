@@ -9,9 +9,7 @@
 // the same arithmetic per point.  The schedule used here:
 //
 //   * every (j,k) line of a slab is owned by one lane; a lane walks its line
-//     in chunks of one 32-byte sector of consecutive i (4 FP64 or 8 FP32
-//     points), so the FP32 sweeps of mixed precision take half the steps
-//     along i;
+//     in chunks of CHUNK=4 consecutive i (one 32-byte sector);
 //   * line (j,k) processes chunk c at logical step T = c + j + k, so its
 //     (j-1) and (k-1) predecessors finished chunk c at step T-1;
 //   * a warp holds 32 consecutive rows of one plane (the j-1 value comes from
@@ -138,7 +136,7 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // row above by shuffle or, for lane 0, from global memory.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
-    constexpr int CH = 32 / (int)sizeof(Val);  // points per lane per step: one 32-byte sector
+    constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
     const Geom& g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const SweepCta cta = a.ctas[blockIdx.x];
@@ -586,7 +584,7 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     a.slabs = h->slabs;
     a.n_cta = h->n_cta;
     a.P = h->P;
-    a.C = (h->g.nx - 2) / (32 / (int)sizeof(T)) + 1;
+    a.C = (h->g.nx - 2) / CHUNK + 1;
     a.flags = h->flags;
     a.epoch = h->epoch++;
     a.err = h->err;
