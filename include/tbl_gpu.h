@@ -343,6 +343,14 @@ const char* tbl_status_string(int status);
 /* Number of kernel launches issued by this handle so far (instrumentation). */
 int64_t tbl_launch_count(tbl_handle* h);
 
+/* Failure-detection self-test (no handle): one kernel thread waits, with the
+ * wavefront sweeps' bounded wait, on a progress flag that nothing sets.  The
+ * wait gives up after its poll limit (about a second) and the kernel reports
+ * TBL_ERR_TIMEOUT in *observed, as a stalled sweep does in tbl_step; the
+ * device stays usable.  Returns TBL_OK when the self-test itself ran;
+ * *seconds (may be NULL) receives the time the wait took. */
+int tbl_selftest_bounded_wait(int32_t* observed, double* seconds);
+
 /* ------------------------------------------------------------ restart files
  * Host-only readers and writers of the reference's restart files (no device,
  * no handle): Tecplot ASCII POINT, i outermost, then j, then k.  Arrays are

@@ -537,6 +537,7 @@ int gmres(Oracle& o, const std::vector<int32_t>* rp, std::vector<int32_t>& count
         double rho = std::sqrt(dot(o, o.r, o.r));
         if (m == 1) {
             sumnor = rho;
+            if (std::isnan(rho)) { status = TBL_ERR_NAN; resid = rho; break; }
             if (!(rho > 0.0)) { status = TBL_ERR_ZERO_RHS; resid = 0.0; break; }
         }
         sumav = rho / sumnor;
@@ -1006,7 +1007,7 @@ int one_step(Oracle& o, tbl_step_stats* st) {
     divergence(o);
     std::vector<int32_t> kits;
     int status = gmres(o, replay ? &rrec : nullptr, kits, s.gmres_restarts, s.gmres_iters, s.gmres_resid);
-    if (status == TBL_ERR_ZERO_RHS) return status;
+    if (status == TBL_ERR_ZERO_RHS || status == TBL_ERR_NAN) return status;
     if (o.c.flags & TBL_FLAG_PPE_RESIDUAL) {
         double num = 0.0, den = 0.0;
         for (int k = 2; k <= o.nz - 1; ++k)

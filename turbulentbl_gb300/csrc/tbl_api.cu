@@ -396,6 +396,7 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
         TRY(readback(h, &h->sc->rho, 4 * sizeof(double)));
         const double rho_m = h->hpin[0];
         if (m == 1) {
+            if (std::isnan(rho_m)) { status = TBL_ERR_NAN; break; }
             if (!(rho_m > 0.0)) { status = TBL_ERR_ZERO_RHS; break; }
             sumnor = rho_m;
         }
@@ -499,6 +500,7 @@ int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_ste
         TRY(launch_restart_init(h, m == 1));
         TRY(readback(h, &h->sc->rho, 4 * sizeof(double)));  // rho, sumnor, sumav
         double rho = h->hpin[0];
+        if (m == 1 && std::isnan(rho)) { status = TBL_ERR_NAN; break; }
         if (m == 1 && !(rho > 0.0)) { status = TBL_ERR_ZERO_RHS; break; }
         sumav = h->hpin[2];
         {
@@ -968,5 +970,15 @@ const char* tbl_status_string(int status) {
 }
 
 int64_t tbl_launch_count(tbl_handle* h) { return h ? h->launches : -1; }
+
+int tbl_selftest_bounded_wait(int32_t* observed, double* seconds) {
+    if (!observed) return TBL_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TBL_ERR_NO_DEVICE;
+    int v = 0;
+    const int st = tbl::selftest_bounded_wait(&v, seconds);
+    *observed = v;
+    return st;
+}
 
 }  // extern "C"

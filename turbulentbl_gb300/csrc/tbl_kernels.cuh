@@ -29,6 +29,7 @@ int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8);
 int launch_ssor_bwd(tbl_handle* h, double* out);
 int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8);
 int launch_ssor_bwd_f(tbl_handle* h, float* out);
+int selftest_bounded_wait(int* observed, double* seconds);
 
 // tbl_krylov.cu
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);

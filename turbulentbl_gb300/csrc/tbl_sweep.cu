@@ -542,6 +542,50 @@ __global__ void __launch_bounds__(256) k_lap(Geom g, TC aw, TC as, const TC* __r
     R[p] = scale ? scale[k] * r : r;
 }
 
+// ------------------------------------------------------ bounded-wait self-test
+// One thread waits, with the sweeps' own bounded wait, on a progress flag that
+// nothing sets; the wait gives up after SPIN_LIMIT polls and reports
+// TBL_ERR_TIMEOUT through the error word, as a stalled sweep warp does.
+__global__ void k_wait_selftest(const unsigned long long* flag, int* err) {
+    if (threadIdx.x != 0) return;
+    if (wait_global(flag, 1ull << 20, 0) < 0) atomicExch(err, TBL_ERR_TIMEOUT);
+}
+
+int selftest_bounded_wait(int* observed, double* seconds) {
+    unsigned long long* flag = nullptr;
+    int* err = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int st = TBL_OK;
+    auto fail = [&](cudaError_t e) { if (e != cudaSuccess && st == TBL_OK) st = TBL_ERR_CUDA; };
+    fail(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    fail(cudaMalloc(&flag, sizeof(unsigned long long)));
+    fail(cudaMalloc(&err, sizeof(int)));
+    fail(cudaEventCreate(&e0));
+    fail(cudaEventCreate(&e1));
+    if (st == TBL_OK) {
+        fail(cudaMemsetAsync(flag, 0, sizeof(unsigned long long), s));
+        fail(cudaMemsetAsync(err, 0, sizeof(int), s));
+        fail(cudaEventRecord(e0, s));
+        k_wait_selftest<<<1, 32, 0, s>>>(flag, err);
+        fail(cudaGetLastError());
+        fail(cudaEventRecord(e1, s));
+        fail(cudaStreamSynchronize(s));
+        int v = 0;
+        fail(cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost));
+        float ms = 0.f;
+        fail(cudaEventElapsedTime(&ms, e0, e1));
+        if (observed) *observed = v;
+        if (seconds) *seconds = ms * 1e-3;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (flag) cudaFree(flag);
+    if (err) cudaFree(err);
+    if (s) cudaStreamDestroy(s);
+    return st;
+}
+
 // ------------------------------------------------------------- host glue
 
 // Build the CTA table for the slab partition (called once at create).
