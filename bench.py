@@ -140,11 +140,13 @@ def dist_setup():
     return world, rank, local
 
 
-def run_cpu(wl, nproc, budget_s, max_steps):
+def run_cpu(wl, nproc, budget_s, max_steps, variant=0):
     """Time the oracle (all host threads) from the seeded field for up to max_steps steps
     or until budget_s seconds are used; at least one step."""
     from oracle.bind import OracleRunner
     mesh, rp, st = make_state(wl, nproc=nproc)
+    if variant:
+        rp.use_variant(variant)
     o = OracleRunner(mesh, rp)
     o.upload(st)
     times, counts = [], []
@@ -170,13 +172,18 @@ def run_cpu(wl, nproc, budget_s, max_steps):
     }
 
 
-def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True, rb=0):
+def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True, rb=0,
+            variant=0):
     """rb: 0 reference ordering, 1 red-black diffusion sweeps, 2 red-black
-    diffusion sweeps and SSOR preconditioner."""
+    diffusion sweeps and SSOR preconditioner.  variant: the reference program
+    the step follows (tbl_config.variant), with that program's cum and
+    recycling start."""
     import torch
     torch.cuda.set_device(local)
     from turbulentbl_gb300.lib import TblGpu
     mesh, rp, st = make_state(wl, nproc=nproc)
+    if variant:
+        rp.use_variant(variant)
     if wl.precision == abi.TBL_PREC_MIXED or rb:
         rp.flags |= abi.TBL_FLAG_PPE_RESIDUAL  # the true ||L7 p' - Q8|| / ||Q8|| every step (one extra pass)
     if rb:
@@ -252,14 +259,14 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
                       "iters": [r["gmres_iters"] for r in e2e_recs]}
     g.close()
     if "mixed_state" in out and rank == 0:
-        out["accuracy"] = mixed_accuracy(wl, nproc, out.pop("mixed_state"), out.pop("mixed_stats"),
+        out["accuracy"] = mixed_accuracy(wl, nproc, variant, out.pop("mixed_state"), out.pop("mixed_stats"),
                                          out["accuracy_steps"], out["recs"])
     if do_cpu and rank == 0:
-        out["cpu"] = run_cpu(wl, nproc, cpu_budget, 1)
+        out["cpu"] = run_cpu(wl, nproc, cpu_budget, 1, variant)
     return out
 
 
-def mixed_accuracy(wl, nproc, dm, sm, nsteps, recs):
+def mixed_accuracy(wl, nproc, variant, dm, sm, nsteps, recs):
     """The state of a mixed-precision or red-black run after nsteps steps
     against the FP64 library in the reference ordering (which matches the FP64
     oracle to 1e-12) from the same seeded start:
@@ -267,6 +274,8 @@ def mixed_accuracy(wl, nproc, dm, sm, nsteps, recs):
     running statistics, plus the worst true PPE residual of the timed steps."""
     from turbulentbl_gb300.lib import TblGpu
     mesh, rp, st = make_state(wl, nproc=nproc)
+    if variant:
+        rp.use_variant(variant)
     rp.precision = abi.TBL_PREC_FP64
     g = TblGpu(mesh, rp)
     g.upload(st)
@@ -360,6 +369,8 @@ def main():
                     help="red-black diffusion sweeps (TBL_FLAG_RB_ORDER): not the reference's sweep order")
     ap.add_argument("--rb-precond", action="store_true",
                     help="with --rb, the SSOR preconditioner red-black ordered too (TBL_FLAG_RB_PRECOND)")
+    ap.add_argument("--variant", type=int, default=0, choices=[0, 1, 2],
+                    help="the reference program the step follows: 0 dnstbl2, 1 originalTBL, 2 dnssetbl")
     ap.add_argument("--adjoint", action="store_true",
                     help="time the discrete adjoint of a window on the 256x96x96 adjoint workload instead")
     ap.add_argument("--window", type=int, default=50)
@@ -398,12 +409,13 @@ def main():
                            if args.rb and args.rb_precond else
                            "red-black Gauss-Seidel, reference block SSOR (throughput mode, not the reference's "
                            "sweep order)" if args.rb else
-                           "reference (lexicographic block Gauss-Seidel / block SSOR)")}
+                           "reference (lexicographic block Gauss-Seidel / block SSOR)"),
+              "program": ["dnstbl2", "originalTBL", "dnssetbl"][args.variant]}
     metric = "Mpt-steps/s"
     if args.impl == "reference":
         if rank != 0:
             return
-        cpu = run_cpu(wl, args.nproc, max(args.cpu_budget, 1.0) * max(args.steps, 1), args.steps)
+        cpu = run_cpu(wl, args.nproc, max(args.cpu_budget, 1.0) * max(args.steps, 1), args.steps, args.variant)
         line = {"metric": metric, "value": cpu["value"], "unit": "Mpt-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": 0, "ms_per_step": cpu["s_per_step"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)",
@@ -416,7 +428,8 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
-                not args.no_cpu, args.cpu_budget, not args.no_accuracy, (2 if args.rb and args.rb_precond else 1 if args.rb else 0))
+                not args.no_cpu, args.cpu_budget, not args.no_accuracy,
+                (2 if args.rb and args.rb_precond else 1 if args.rb else 0), args.variant)
     if rank != 0:
         return
     K = args.steps
