@@ -318,15 +318,20 @@ __device__ __forceinline__ float dot4f(float4 a, float4 b) {
 // d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the G basis vectors of group
 // blockIdx.y (first vector g0 + G*blockIdx.y).  Each thread sums its FP32
 // products over its share of the points (a few float4 at most) and converts
-// once; blocks reduce in FP64 and the last block of each group sums the
-// partials in block order (deterministic).
+// once.  A block reduces its 2G values together (one shuffle tree per value,
+// one barrier), writes the 2G partials, and the last block of the group sums
+// each value's partials with one warp (lanes strided over the blocks, four
+// loads in flight per lane, then the shuffle tree): a fixed order, so the
+// result is deterministic.  Reducing the values one block-wide sum at a time
+// cost about as much as the loads of the pass.
 template <int G>
 __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
                                                             const float4* __restrict__ V, long long vstride4, int nv,
                                                             int g0, double* __restrict__ partial,
                                                             unsigned int* __restrict__ count, int max_blocks,
                                                             double* __restrict__ dout, double* __restrict__ gout) {
-    __shared__ double s_red[RED_THREADS / 32];
+    constexpr int NW = RED_THREADS / 32;
+    __shared__ double s_red[2 * G * NW];
     __shared__ bool s_last;
     const int grp = g0 / LSG_G + blockIdx.y;  // slot index of this group
     const int i0 = g0 + blockIdx.y * G;
@@ -344,28 +349,42 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
             fg[e] += dot4f(v, l);
         }
     }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const size_t base = (size_t)grp * 2 * LSG_G;
 #pragma unroll
     for (int e = 0; e < G; ++e) {
-        const double bd = block_sum((double)fd[e], s_red);
-        const double bg = block_sum((double)fg[e], s_red);
-        if (threadIdx.x == 0) {
-            partial[(base + 2 * e) * max_blocks + blockIdx.x] = bd;
-            partial[(base + 2 * e + 1) * max_blocks + blockIdx.x] = bg;
+        const double a = warp_sum((double)fd[e]), b = warp_sum((double)fg[e]);
+        if (lane == 0) {
+            s_red[(2 * e) * NW + wid] = a;
+            s_red[(2 * e + 1) * NW + wid] = b;
         }
     }
-    if (threadIdx.x == 0) {
+    __syncthreads();
+    if (threadIdx.x < 2 * G) {
+        double a = 0.0;
+        for (int q = 0; q < NW; ++q) a += s_red[threadIdx.x * NW + q];
+        partial[(base + threadIdx.x) * max_blocks + blockIdx.x] = a;
         __threadfence();
-        s_last = atomicAdd(&count[grp], 1u) == gridDim.x - 1;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&count[grp], 1u) == gridDim.x - 1;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    for (int v = 0; v < 2 * G; ++v) {
-        double acc = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&partial[(base + v) * max_blocks + b]);
-        acc = block_sum(acc, s_red);
-        if (threadIdx.x == 0) {
+    const int nb = (int)gridDim.x;
+    for (int v = wid; v < 2 * G; v += NW) {
+        const double* p = partial + (base + v) * max_blocks;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int b = lane;
+        for (; b + 96 < nb; b += 128) {
+            a0 += __ldcg(p + b);
+            a1 += __ldcg(p + b + 32);
+            a2 += __ldcg(p + b + 64);
+            a3 += __ldcg(p + b + 96);
+        }
+        for (; b < nb; b += 32) a0 += __ldcg(p + b);
+        const double acc = warp_sum((a0 + a1) + (a2 + a3));
+        if (lane == 0) {
             const int i = i0 + v / 2;
             if (v % 2 == 0) dout[i] = acc;
             else if (i < nv - 1) gout[i] = acc;
