@@ -173,7 +173,7 @@ def run_cpu(wl, nproc, budget_s, max_steps, variant=0):
 
 
 def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_budget, do_accuracy=True, rb=0,
-            variant=0):
+            variant=0, extra_flags=0):
     """rb: 0 reference ordering, 1 red-black diffusion sweeps, 2 red-black
     diffusion sweeps and SSOR preconditioner.  variant: the reference program
     the step follows (tbl_config.variant), with that program's cum and
@@ -190,6 +190,9 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
         rp.flags |= abi.TBL_FLAG_RB_ORDER
     if rb > 1:
         rp.flags |= abi.TBL_FLAG_RB_PRECOND
+    rp.flags |= extra_flags
+    if extra_flags:
+        rp.flags |= abi.TBL_FLAG_PPE_RESIDUAL
     g = TblGpu(mesh, rp)
     g.upload(st)
     for _ in range(warmup):
@@ -225,7 +228,7 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launch_groups": nl[q]} for q in range(ng - 1)}
     out = {"elapsed": elapsed, "host_elapsed": e1 - e0, "recs": recs, "status": st_all, "launches": launches,
            "clocks": clk, "groups": groups}
-    if (wl.precision == abi.TBL_PREC_MIXED or rb) and do_accuracy:
+    if (wl.precision == abi.TBL_PREC_MIXED or rb or extra_flags) and do_accuracy:
         out["mixed_state"] = g.download(fields=("u", "v", "w", "p"))
         out["mixed_stats"] = g.download_stats()
         out["accuracy_steps"] = warmup + steps
@@ -369,6 +372,8 @@ def main():
                     help="red-black diffusion sweeps (TBL_FLAG_RB_ORDER): not the reference's sweep order")
     ap.add_argument("--rb-precond", action="store_true",
                     help="with --rb, the SSOR preconditioner red-black ordered too (TBL_FLAG_RB_PRECOND)")
+    ap.add_argument("--span-blocks", action="store_true",
+                    help="block SSOR on 32-row span blocks (TBL_FLAG_SSOR_SPAN_BLOCKS): not the reference's preconditioner")
     ap.add_argument("--variant", type=int, default=0, choices=[0, 1, 2],
                     help="the reference program the step follows: 0 dnstbl2, 1 originalTBL, 2 dnssetbl")
     ap.add_argument("--adjoint", action="store_true",
@@ -410,7 +415,9 @@ def main():
                            "red-black Gauss-Seidel, reference block SSOR (throughput mode, not the reference's "
                            "sweep order)" if args.rb else
                            "reference (lexicographic block Gauss-Seidel / block SSOR)"),
-              "program": ["dnstbl2", "originalTBL", "dnssetbl"][args.variant]}
+              "program": ["dnstbl2", "originalTBL", "dnssetbl"][args.variant],
+              "preconditioner": ("block SSOR on slabs x 32-row span blocks (throughput mode, not the reference's)"
+                                 if args.span_blocks else "block SSOR on the slabs (reference)")}
     metric = "Mpt-steps/s"
     if args.impl == "reference":
         if rank != 0:
@@ -429,7 +436,8 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
                 not args.no_cpu, args.cpu_budget, not args.no_accuracy,
-                (2 if args.rb and args.rb_precond else 1 if args.rb else 0), args.variant)
+                (2 if args.rb and args.rb_precond else 1 if args.rb else 0), args.variant,
+                abi.TBL_FLAG_SSOR_SPAN_BLOCKS if args.span_blocks else 0)
     if rank != 0:
         return
     K = args.steps

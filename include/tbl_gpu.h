@@ -84,6 +84,10 @@ extern "C" {
 #define TBL_FLAG_RB_PRECOND   16  /* with TBL_FLAG_RB_ORDER: the SSOR preconditioner of GMRES red-black ordered
                                      too.  A weaker preconditioner (about 2.7x the GMRES iterations at
                                      512x128x128), kept for experiments */
+#define TBL_FLAG_SSOR_SPAN_BLOCKS 32  /* throughput mode, not the reference's preconditioner: the block SSOR of
+                                     GMRES also splits every slab into blocks of 32 span rows (zero halos
+                                     between blocks, as between slabs), so a preconditioner sweep is
+                                     nx/4 + 32 + K wavefront steps long instead of nx/4 + (ny-2) + K */
 #define TBL_FLAG_DIAGNOSTICS   4  /* accepted for compatibility: the divergence, mass-flux, wall-shear and
                                      KE diagnostics run every step, as in the reference */
 

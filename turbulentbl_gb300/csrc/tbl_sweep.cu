@@ -54,6 +54,7 @@ struct SweepArgs {
     T* halo_out;
     // SSOR
     double omega, sw;           // w, (2-w)/w
+    int jb_rows;                // SSOR: rows per span block (a multiple of 32; 0 = one block per slab)
     const T* X;                 // matvec input (FWD) / PCorr (FWD residual mode)
     const double* Q8;           // residual mode when non-null
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
@@ -152,6 +153,10 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     __syncthreads();
 
     const int jl = 32 * cta.jb + lane;  // logical row
+    // SSOR with span blocks: rows restart the schedule at every block of
+    // jb_rows rows (the row before a block reads zero, as across slabs)
+    const int jblk0 = (MODE != SW_GS && a.jb_rows > 0) ? (32 * cta.jb / a.jb_rows) * a.jb_rows : 0;
+    const int jr = jl - jblk0;          // row within its span block
     const int kl = KG * cta.kg + wid;   // logical plane
     if (kl >= K) return;                // no lines: nobody waits for this warp
     const bool line_ok = jl < J;
@@ -163,13 +168,14 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
     const long long sy = g.sx;
 
-    const int jl_last = min(32 * cta.jb + 31, J - 1);
-    const int T0 = 32 * cta.jb + kl;
+    const int jl_last = min(32 * cta.jb + 31, J - 1) - jblk0;  // within the span block
+    const int T0 = 32 * cta.jb - jblk0 + kl;
     const int T1 = jl_last + kl + C - 1;
     const int tend_k = T1 - 1;          // last step of the (k-1) upstream warp
-    const int tend_j = 32 * cta.jb - 1 + kl + C - 1;
+    const int tend_j = 32 * cta.jb - jblk0 - 1 + kl + C - 1;
     const bool has_down = wid < KG - 1 && kl + 1 < K;
-    const unsigned long long* fj = cta.up_j >= 0 ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
+    const unsigned long long* fj =
+        (cta.up_j >= 0 && 32 * cta.jb != jblk0) ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
     const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
     unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
     const unsigned long long tag = a.epoch << 20;
@@ -214,7 +220,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         Val* io = MODE == SW_FWD ? a.RH : a.OUT;
         kin_zero = MODE == SW_FWD ? (kidx == 0) : (kidx == K - 1);
         kin = io + line + (MODE == SW_FWD ? -g.ps : g.ps);
-        jin_zero = MODE == SW_FWD ? (jidx == 0) : (jidx == J - 1);
+        jin_zero = jr == 0;  // the first row of the slab (FWD: j = 1; BWD: j = J) or of a span block
         jin = io + sy * ((long long)(jin_zero ? j : (MODE == SW_FWD ? j - 1 : j + 1)) + (long long)g.ny * k);
     }
     Val* outp = MODE == SW_GS ? F : (MODE == SW_FWD ? a.RH : a.OUT) + line;
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
     auto load_raw = [&](int ts) {
-        const int cl = ts - jl - kl;
+        const int cl = ts - jr - kl;
         if (!line_ok || cl < 0 || cl >= C) return;
         const int i0 = CH * (MODE == SW_BWD ? C - 1 - cl : cl);
 #pragma unroll
@@ -240,7 +246,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     };
     Val pre[CH];
     auto make_pre = [&](int ts) {
-        const int cl = ts - jl - kl;
+        const int cl = ts - jr - kl;
         if (!line_ok || cl < 0 || cl >= C) return;
 #pragma unroll
         for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
@@ -253,7 +259,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     int abort = 0;
 
     for (int T = T0; T <= T1; ++T) {
-        const int cl = T - jl - kl;
+        const int cl = T - jr - kl;
         const bool act = line_ok && cl >= 0 && cl < C;
         const int c = MODE == SW_BWD ? C - 1 - cl : cl;
         const int i0 = CH * c;
@@ -265,7 +271,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         load_raw(T + 1);
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
         if (lane == 0) {
-            const int cl0 = T - 32 * cta.jb - kl;
+            const int cl0 = T - (32 * cta.jb - jblk0) - kl;
             if (fj && cl0 >= 0 && cl0 < C && !pj_ok && seen_j < T - 1) {
                 seen_j = wait_global(fj, tag, T - 1);
                 if (seen_j < 0) abort = 1;
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         pj_ok = false;
         pk_ok = false;
         if (T < T1) {
-            const int cln = T + 1 - jl - kl;
+            const int cln = T + 1 - jr - kl;
             const bool actn = line_ok && cln >= 0 && cln < C;
             const int i0n = CH * (MODE == SW_BWD ? C - 1 - cln : cln);
             if (lane == 0 && fj && seen_j >= T && actn) {
@@ -637,6 +643,7 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     a.as = 1.0 / (h->cfg.dy * h->cfg.dy);
     a.omega = h->cfg.omega;
     a.sw = (2 - h->cfg.omega) / h->cfg.omega;
+    a.jb_rows = (h->cfg.flags & TBL_FLAG_SSOR_SPAN_BLOCKS) ? 32 : 0;
     a.t = -h->cfg.dt / (h->cfg.re);
     return a;
 }
