@@ -374,6 +374,9 @@ def main():
                     help="with --rb, the SSOR preconditioner red-black ordered too (TBL_FLAG_RB_PRECOND)")
     ap.add_argument("--span-blocks", action="store_true",
                     help="block SSOR on 32-row span blocks (TBL_FLAG_SSOR_SPAN_BLOCKS): not the reference's preconditioner")
+    ap.add_argument("--stream-blocks", action="store_true",
+                    help="block SSOR on two streamwise blocks per line (TBL_FLAG_SSOR_STREAM_BLOCKS): not the "
+                         "reference's preconditioner")
     ap.add_argument("--variant", type=int, default=0, choices=[0, 1, 2],
                     help="the reference program the step follows: 0 dnstbl2, 1 originalTBL, 2 dnssetbl")
     ap.add_argument("--adjoint", action="store_true",
@@ -416,8 +419,10 @@ def main():
                            "sweep order)" if args.rb else
                            "reference (lexicographic block Gauss-Seidel / block SSOR)"),
               "program": ["dnstbl2", "originalTBL", "dnssetbl"][args.variant],
-              "preconditioner": ("block SSOR on slabs x 32-row span blocks (throughput mode, not the reference's)"
-                                 if args.span_blocks else "block SSOR on the slabs (reference)")}
+              "preconditioner": ("block SSOR on the slabs (reference)" if not (args.span_blocks or args.stream_blocks)
+                                 else "block SSOR on slabs" + (" x 32-row span blocks" if args.span_blocks else "")
+                                 + (" x 2 streamwise blocks" if args.stream_blocks else "")
+                                 + " (throughput mode, not the reference's)")}
     metric = "Mpt-steps/s"
     if args.impl == "reference":
         if rank != 0:
@@ -437,7 +442,8 @@ def main():
     r = run_gpu(wl, args.nproc, args.steps, max(args.warmup, 3), world, rank, local, not args.no_e2e,
                 not args.no_cpu, args.cpu_budget, not args.no_accuracy,
                 (2 if args.rb and args.rb_precond else 1 if args.rb else 0), args.variant,
-                abi.TBL_FLAG_SSOR_SPAN_BLOCKS if args.span_blocks else 0)
+                (abi.TBL_FLAG_SSOR_SPAN_BLOCKS if args.span_blocks else 0) |
+                (abi.TBL_FLAG_SSOR_STREAM_BLOCKS if args.stream_blocks else 0))
     if rank != 0:
         return
     K = args.steps

@@ -48,6 +48,7 @@ TBL_FLAG_DIAGNOSTICS = 4
 TBL_FLAG_RB_ORDER = 8
 TBL_FLAG_RB_PRECOND = 16
 TBL_FLAG_SSOR_SPAN_BLOCKS = 32
+TBL_FLAG_SSOR_STREAM_BLOCKS = 64
 
 TBL_VARIANT_DNSTBL2 = 0
 TBL_VARIANT_ORIGINAL = 1

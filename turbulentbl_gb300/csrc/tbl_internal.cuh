@@ -157,6 +157,7 @@ struct tbl_handle {
     double time;
     bool fluc_updated;
     int coop_ok;
+    int ssor_nib;                  // streamwise SSOR blocks per slab (TBL_FLAG_SSOR_STREAM_BLOCKS), 1 or 2
     int gs_comps_per_launch;       // velocity components one cooperative GS launch can hold (1..3)
     int n_sm;                      // multiprocessors of the device
     // replay

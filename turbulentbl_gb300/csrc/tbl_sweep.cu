@@ -55,6 +55,7 @@ struct SweepArgs {
     // SSOR
     double omega, sw;           // w, (2-w)/w
     int jb_rows;                // SSOR: rows per span block (a multiple of 32; 0 = one block per slab)
+    int nib;                    // SSOR: streamwise blocks (grid.y), 1 = one block per line
     const T* X;                 // matvec input (FWD) / PCorr (FWD residual mode)
     const double* Q8;           // residual mode when non-null
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
@@ -145,6 +146,14 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     const int J = g.ny - 2, K = sl.K;
     const int C = (g.nx - 2) / CH + 1;     // chunks per line
     const int compi = blockIdx.y;
+    // SSOR with streamwise blocks: grid.y picks the block of chunks
+    // [c_lo, c_hi] this CTA sweeps (zero halo at its start, as across slabs);
+    // each block has its own progress flags (the per-component flag sets)
+    const int nib = MODE != SW_GS ? a.nib : 1;
+    const int CB = (C + nib - 1) / nib;
+    const int c_lo = MODE != SW_GS ? (int)blockIdx.y * CB : 0;
+    const int c_hi = min(C, c_lo + CB) - 1;
+    const int Cl = c_hi - c_lo + 1;        // chunks of this block
     const int comp = MODE == SW_GS ? a.comp[compi] : 0;
     unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
     __shared__ int s_prog[KG];
@@ -170,9 +179,9 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
 
     const int jl_last = min(32 * cta.jb + 31, J - 1) - jblk0;  // within the span block
     const int T0 = 32 * cta.jb - jblk0 + kl;
-    const int T1 = jl_last + kl + C - 1;
+    const int T1 = jl_last + kl + Cl - 1;
     const int tend_k = T1 - 1;          // last step of the (k-1) upstream warp
-    const int tend_j = 32 * cta.jb - jblk0 - 1 + kl + C - 1;
+    const int tend_j = 32 * cta.jb - jblk0 - 1 + kl + Cl - 1;
     const bool has_down = wid < KG - 1 && kl + 1 < K;
     const unsigned long long* fj =
         (cta.up_j >= 0 && 32 * cta.jb != jblk0) ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
@@ -239,15 +248,15 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
     auto load_raw = [&](int ts) {
         const int cl = ts - jr - kl;
-        if (!line_ok || cl < 0 || cl >= C) return;
-        const int i0 = CH * (MODE == SW_BWD ? C - 1 - cl : cl);
+        if (!line_ok || cl < 0 || cl >= Cl) return;
+        const int i0 = CH * (MODE == SW_BWD ? c_hi - cl : c_lo + cl);
 #pragma unroll
         for (int e = 0; e < CH; ++e) ra[e] = inp[i0 + e];
     };
     Val pre[CH];
     auto make_pre = [&](int ts) {
         const int cl = ts - jr - kl;
-        if (!line_ok || cl < 0 || cl >= C) return;
+        if (!line_ok || cl < 0 || cl >= Cl) return;
 #pragma unroll
         for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
     };
@@ -260,10 +269,11 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
 
     for (int T = T0; T <= T1; ++T) {
         const int cl = T - jr - kl;
-        const bool act = line_ok && cl >= 0 && cl < C;
-        const int c = MODE == SW_BWD ? C - 1 - cl : cl;
+        const bool act = line_ok && cl >= 0 && cl < Cl;
+        const int c = MODE == SW_BWD ? c_hi - cl : c_lo + cl;
         const int i0 = CH * c;
         const bool edge = (c == 0) || (c == C - 1);
+        if (cl == 0) carry = Val(0);  // first chunk of the line in this block: nothing before it
         Val cur[CH];
 #pragma unroll
         for (int e = 0; e < CH; ++e) cur[e] = pre[e];
@@ -272,11 +282,11 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
         if (lane == 0) {
             const int cl0 = T - (32 * cta.jb - jblk0) - kl;
-            if (fj && cl0 >= 0 && cl0 < C && !pj_ok && seen_j < T - 1) {
+            if (fj && cl0 >= 0 && cl0 < Cl && !pj_ok && seen_j < T - 1) {
                 seen_j = wait_global(fj, tag, T - 1);
                 if (seen_j < 0) abort = 1;
             }
-            if (kl > 0 && cl0 >= 0 && T - jl_last - kl < C) {
+            if (kl > 0 && cl0 >= 0 && T - jl_last - kl < Cl) {
                 const int target = min(T - 1, tend_k);
                 if (wid > 0) {
                     if (!wait_cta(&s_prog[wid - 1], target)) abort = 1;
@@ -382,8 +392,8 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         pk_ok = false;
         if (T < T1) {
             const int cln = T + 1 - jr - kl;
-            const bool actn = line_ok && cln >= 0 && cln < C;
-            const int i0n = CH * (MODE == SW_BWD ? C - 1 - cln : cln);
+            const bool actn = line_ok && cln >= 0 && cln < Cl;
+            const int i0n = CH * (MODE == SW_BWD ? c_hi - cln : c_lo + cln);
             if (lane == 0 && fj && seen_j >= T && actn) {
 #pragma unroll
                 for (int e = 0; e < CH; ++e) pj_pf[e] = jin_zero ? Val(0) : __ldcg(jin + i0n + e);
@@ -644,6 +654,7 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     a.omega = h->cfg.omega;
     a.sw = (2 - h->cfg.omega) / h->cfg.omega;
     a.jb_rows = (h->cfg.flags & TBL_FLAG_SSOR_SPAN_BLOCKS) ? 32 : 0;
+    a.nib = h->ssor_nib > 0 ? h->ssor_nib : 1;
     a.t = -h->cfg.dt / (h->cfg.re);
     return a;
 }
@@ -741,7 +752,7 @@ int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
-    return launch_sweep<SW_FWD, double>(h, a, 1);
+    return launch_sweep<SW_FWD, double>(h, a, a.nib);
 }
 
 template <typename T>
@@ -763,7 +774,7 @@ int launch_ssor_bwd(tbl_handle* h, double* out) {
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     a.OUT = out;
-    return launch_sweep<SW_BWD, double>(h, a, 1);
+    return launch_sweep<SW_BWD, double>(h, a, a.nib);
 }
 
 // Mixed precision: FP32 preconditioned matvec of the inner GMRES.  Xd (FP64
@@ -783,7 +794,7 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
-    return launch_sweep<SW_FWD, float>(h, a, 1);
+    return launch_sweep<SW_FWD, float>(h, a, a.nib);
 }
 
 int launch_ssor_bwd_f(tbl_handle* h, float* out) {
@@ -795,7 +806,7 @@ int launch_ssor_bwd_f(tbl_handle* h, float* out) {
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
     a.OUT = out;
-    return launch_sweep<SW_BWD, float>(h, a, 1);
+    return launch_sweep<SW_BWD, float>(h, a, a.nib);
 }
 
 // Snapshot of the planes every slab reads from its neighbours before the
@@ -854,6 +865,13 @@ int check_cooperative(tbl_handle* h) {
     h->coop_ok = coop && cap[0] >= h->n_cta && cap[1] >= h->n_cta && cap[2] >= h->n_cta;
     h->gs_comps_per_launch = (int)(cap[0] / (h->n_cta > 0 ? h->n_cta : 1));
     if (h->gs_comps_per_launch > 3) h->gs_comps_per_launch = 3;
+    // streamwise SSOR blocks: as many as requested that stay co-resident (at
+    // most 3: the flag sets of the three GS components are reused)
+    h->ssor_nib = 1;
+    if (h->cfg.flags & TBL_FLAG_SSOR_STREAM_BLOCKS) {
+        const long long fit = (cap[1] < cap[2] ? cap[1] : cap[2]) / (h->n_cta > 0 ? h->n_cta : 1);
+        h->ssor_nib = fit >= 2 ? 2 : 1;
+    }
     return h->coop_ok ? TBL_OK : TBL_ERR_BAD_ARG;
 }
 
