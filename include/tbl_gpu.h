@@ -89,9 +89,9 @@ extern "C" {
                                      between blocks, as between slabs), so a preconditioner sweep is
                                      nx/4 + 32 + K wavefront steps long instead of nx/4 + (ny-2) + K */
 #define TBL_FLAG_SSOR_STREAM_BLOCKS 64  /* throughput mode, not the reference's preconditioner: the block SSOR
-                                     also splits every line into two streamwise blocks (zero halo between
-                                     them), halving the nx/4 part of the wavefront chain; one block when the
-                                     doubled sweep would not be co-resident */
+                                     also splits every line into up to four streamwise blocks (zero halo
+                                     between them), as many as keep the sweep's CTAs co-resident, cutting the
+                                     nx/4 part of the wavefront chain */
 #define TBL_FLAG_DIAGNOSTICS   4  /* accepted for compatibility: the divergence, mass-flux, wall-shear and
                                      KE diagnostics run every step, as in the reference */
 

@@ -27,6 +27,7 @@ void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int 
 
 constexpr int CHUNK = 4;          // i-points per lane per wavefront step
 constexpr int KG = 4;             // k-planes (warps) per wavefront CTA
+constexpr int SSOR_MAX_NIB = 4;    // streamwise SSOR blocks per line at most
 constexpr int RED_THREADS = 256;  // threads per reduction block
 
 // Geometry shared by all kernels (passed by value).
@@ -157,7 +158,7 @@ struct tbl_handle {
     double time;
     bool fluc_updated;
     int coop_ok;
-    int ssor_nib;                  // streamwise SSOR blocks per slab (TBL_FLAG_SSOR_STREAM_BLOCKS), 1 or 2
+    int ssor_nib;                  // streamwise SSOR blocks per line (TBL_FLAG_SSOR_STREAM_BLOCKS), 1..SSOR_MAX_NIB
     int gs_comps_per_launch;       // velocity components one cooperative GS launch can hold (1..3)
     int n_sm;                      // multiprocessors of the device
     // replay

@@ -629,8 +629,10 @@ int build_sweep_ctas(tbl_handle* h) {
     TBL_CUDA_TRY(cudaMemcpy(h->ctas, ctas.data(), ctas.size() * sizeof(SweepCta), cudaMemcpyHostToDevice));
     TBL_CUDA_TRY(cudaMalloc(&h->slabs, slabs.size() * sizeof(SlabDesc)));
     TBL_CUDA_TRY(cudaMemcpy(h->slabs, slabs.data(), slabs.size() * sizeof(SlabDesc), cudaMemcpyHostToDevice));
-    TBL_CUDA_TRY(cudaMalloc(&h->flags, (size_t)3 * h->n_cta * KG * sizeof(unsigned long long)));
-    TBL_CUDA_TRY(cudaMemset(h->flags, 0, (size_t)3 * h->n_cta * KG * sizeof(unsigned long long)));
+    // flag sets: three GS components, or up to SSOR_MAX_NIB streamwise SSOR blocks
+    const size_t nsets = SSOR_MAX_NIB > 3 ? SSOR_MAX_NIB : 3;
+    TBL_CUDA_TRY(cudaMalloc(&h->flags, nsets * h->n_cta * KG * sizeof(unsigned long long)));
+    TBL_CUDA_TRY(cudaMemset(h->flags, 0, nsets * h->n_cta * KG * sizeof(unsigned long long)));
     h->epoch = 1;
     return TBL_OK;
 }
@@ -865,12 +867,16 @@ int check_cooperative(tbl_handle* h) {
     h->coop_ok = coop && cap[0] >= h->n_cta && cap[1] >= h->n_cta && cap[2] >= h->n_cta;
     h->gs_comps_per_launch = (int)(cap[0] / (h->n_cta > 0 ? h->n_cta : 1));
     if (h->gs_comps_per_launch > 3) h->gs_comps_per_launch = 3;
-    // streamwise SSOR blocks: as many as requested that stay co-resident (at
-    // most 3: the flag sets of the three GS components are reused)
+    // streamwise SSOR blocks: up to SSOR_MAX_NIB, as many as stay co-resident
     h->ssor_nib = 1;
     if (h->cfg.flags & TBL_FLAG_SSOR_STREAM_BLOCKS) {
         const long long fit = (cap[1] < cap[2] ? cap[1] : cap[2]) / (h->n_cta > 0 ? h->n_cta : 1);
-        h->ssor_nib = fit >= 2 ? 2 : 1;
+        int nib = (int)(fit < SSOR_MAX_NIB ? (fit < 1 ? 1 : fit) : SSOR_MAX_NIB);
+        // no empty block: the sweep splits C chunks into blocks of ceil(C/nib)
+        const int C = (h->g.nx - 2) / 4 + 1;
+        if (nib > C) nib = C;
+        const int cb = (C + nib - 1) / nib;
+        h->ssor_nib = (C + cb - 1) / cb;
     }
     return h->coop_ok ? TBL_OK : TBL_ERR_BAD_ARG;
 }
