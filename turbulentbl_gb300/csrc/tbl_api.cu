@@ -112,7 +112,7 @@ static int dalloc(T** p, size_t n) {
 
 static void free_all(tbl_handle* h) {
     void* mptrs[] = {h->Uf[0], h->Uf[1], h->Uf[2], h->Pf, h->Qf[0], h->Qf[1], h->Qf[2], h->Df[0], h->Df[1],
-                     h->Df[2], h->Vf, h->RHf, h->R64, h->PREf, h->PRE, h->lsg_partial, h->lsg_count, h->lsg_L, h->lsg_d, h->lsg_g};
+                     h->Df[2], h->Vf, h->RHf, h->R64, h->PREf, h->PRE, h->lsg_partial, h->lsg_L, h->lsg_d, h->lsg_g};
     for (void* p : mptrs)
         if (p) cudaFree(p);
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
@@ -199,7 +199,6 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
         TRY(dalloc(&h->Vf, vol * (size_t)(cfg->mixed_kmax + 1)));
         const int K1m = cfg->mixed_kmax + 1, ngr = (K1m + 7) / 8;
         TRY(dalloc(&h->lsg_partial, (size_t)2 * 8 * ngr * 2048));
-        TRY(dalloc(&h->lsg_count, (size_t)ngr));
         TRY(dalloc(&h->lsg_L, (size_t)K1m * K1m));
         TRY(dalloc(&h->lsg_d, (size_t)K1m));
         TRY(dalloc(&h->lsg_g, (size_t)K1m));

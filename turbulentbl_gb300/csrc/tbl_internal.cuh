@@ -113,7 +113,6 @@ struct tbl_handle {
     float* RHf;      // inner SSOR work
     double* R64;     // FP64 outer residual
     double* lsg_partial;        // low-synch Gram-Schmidt: per-block partials [2*8*groups][max_blocks]
-    unsigned int* lsg_count;    // arrival counters per group
     double *lsg_L, *lsg_d, *lsg_g;  // (K1 x K1) strictly lower Gram matrix, Q^T w, Q^T v_new
     // per-k coefficient arrays and mesh (nz)
     double *x3, *jacinv, *jac2, *Ab, *At, *Ap, *rAp;

@@ -317,22 +317,18 @@ __device__ __forceinline__ float dot4f(float4 a, float4 b) {
 
 // d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the G basis vectors of group
 // blockIdx.y (first vector g0 + G*blockIdx.y).  Each thread sums its FP32
-// products over its share of the points (a few float4 at most) and converts
-// once.  A block reduces its 2G values together (one shuffle tree per value,
-// one barrier), writes the 2G partials, and the last block of the group sums
-// each value's partials with one warp (lanes strided over the blocks, four
-// loads in flight per lane, then the shuffle tree): a fixed order, so the
-// result is deterministic.  Reducing the values one block-wide sum at a time
-// cost about as much as the loads of the pass.
+// products over its share of the points (a few float4 at most); the block
+// sums its 2G values with an FP32 shuffle tree per warp and FP64 over the
+// warps, and writes 2G partials.  k_lsg_reduce then sums each value's
+// partials in FP64 (fixed order: deterministic).  Finishing in the last
+// block (a fence, an atomic, then the 2G sums) and FP64 shuffle trees cost
+// as much as the pass's loads.
 template <int G>
 __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
                                                             const float4* __restrict__ V, long long vstride4, int nv,
-                                                            int g0, double* __restrict__ partial,
-                                                            unsigned int* __restrict__ count, int max_blocks,
-                                                            double* __restrict__ dout, double* __restrict__ gout) {
+                                                            int g0, double* __restrict__ partial, int max_blocks) {
     constexpr int NW = RED_THREADS / 32;
-    __shared__ double s_red[2 * G * NW];
-    __shared__ bool s_last;
+    __shared__ float s_red[2 * G * NW];
     const int grp = g0 / LSG_G + blockIdx.y;  // slot index of this group
     const int i0 = g0 + blockIdx.y * G;
     const float4* vl = V + (long long)(nv - 1) * vstride4;
@@ -350,10 +346,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
         }
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const size_t base = (size_t)grp * 2 * LSG_G;
 #pragma unroll
     for (int e = 0; e < G; ++e) {
-        const double a = warp_sum((double)fd[e]), b = warp_sum((double)fg[e]);
+        const float a = warp_sum(fd[e]), b = warp_sum(fg[e]);
         if (lane == 0) {
             s_red[(2 * e) * NW + wid] = a;
             s_red[(2 * e + 1) * NW + wid] = b;
@@ -362,35 +357,36 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
     __syncthreads();
     if (threadIdx.x < 2 * G) {
         double a = 0.0;
-        for (int q = 0; q < NW; ++q) a += s_red[threadIdx.x * NW + q];
-        partial[(base + threadIdx.x) * max_blocks + blockIdx.x] = a;
-        __threadfence();
+        for (int q = 0; q < NW; ++q) a += (double)s_red[threadIdx.x * NW + q];
+        partial[((size_t)grp * 2 * LSG_G + threadIdx.x) * max_blocks + blockIdx.x] = a;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&count[grp], 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    const int nb = (int)gridDim.x;
-    for (int v = wid; v < 2 * G; v += NW) {
-        const double* p = partial + (base + v) * max_blocks;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        int b = lane;
-        for (; b + 96 < nb; b += 128) {
-            a0 += __ldcg(p + b);
-            a1 += __ldcg(p + b + 32);
-            a2 += __ldcg(p + b + 64);
-            a3 += __ldcg(p + b + 96);
-        }
-        for (; b < nb; b += 32) a0 += __ldcg(p + b);
-        const double acc = warp_sum((a0 + a1) + (a2 + a3));
-        if (lane == 0) {
-            const int i = i0 + v / 2;
-            if (v % 2 == 0) dout[i] = acc;
-            else if (i < nv - 1) gout[i] = acc;
-        }
+}
+
+// The 2 nv values of the dot pass: one warp per value sums its nb block
+// partials (lanes strided over the blocks, four loads in flight per lane,
+// then the shuffle tree); d[i] for even slots, g[i] (i < nv-1) for odd.
+__global__ void __launch_bounds__(256) k_lsg_reduce(const double* __restrict__ partial, int max_blocks, int nb,
+                                                    int nv, double* __restrict__ dout, double* __restrict__ gout) {
+    const int lane = threadIdx.x & 31;
+    const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // value 0 .. 2 nv - 1
+    if (v >= 2 * nv) return;
+    const int grp = v / (2 * LSG_G), within = v % (2 * LSG_G);
+    const double* p = partial + ((size_t)grp * 2 * LSG_G + within) * max_blocks;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int b = lane;
+    for (; b + 96 < nb; b += 128) {
+        a0 += p[b];
+        a1 += p[b + 32];
+        a2 += p[b + 64];
+        a3 += p[b + 96];
     }
-    if (threadIdx.x == 0) count[grp] = 0u;
+    for (; b < nb; b += 32) a0 += p[b];
+    const double acc = warp_sum((a0 + a1) + (a2 + a3));
+    if (lane == 0) {
+        const int i = grp * LSG_G + within / 2;
+        if (within % 2 == 0) dout[i] = acc;
+        else if (i < nv - 1) gout[i] = acc;
+    }
 }
 
 // New row of L (row nv-1: <v_{nv-1}, v_j>, j < nv-1), then (I + L) t = d by
@@ -459,28 +455,29 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
     const float4* Wc = (const float4*)W;
     const float4* Vc = (const float4*)h->Vf;
     if (nfull > 0)
-        k_lsg_dots_f<LSG_G><<<dim3(nbd, nfull), RED_THREADS, 0, h->stream>>>(
-            n4, Wc, Vc, n4, kit, 0, h->lsg_partial, h->lsg_count, h->red.max_blocks, h->lsg_d, h->lsg_g);
+        k_lsg_dots_f<LSG_G><<<dim3(nbd, nfull), RED_THREADS, 0, h->stream>>>(n4, Wc, Vc, n4, kit, 0,
+                                                                             h->lsg_partial, h->red.max_blocks);
     if (rem > 0) {
         const int g0 = nfull * LSG_G;
         switch (rem) {
 #define TBL_LSG_REM(R)                                                                                              \
     case R:                                                                                                         \
         k_lsg_dots_f<R><<<dim3(nbd, 1), RED_THREADS, 0, h->stream>>>(n4, Wc, Vc, n4, kit, g0, h->lsg_partial,       \
-                                                                    h->lsg_count, h->red.max_blocks, h->lsg_d,     \
-                                                                    h->lsg_g);                                      \
+                                                                    h->red.max_blocks);                            \
         break;
             TBL_LSG_REM(1) TBL_LSG_REM(2) TBL_LSG_REM(3) TBL_LSG_REM(4) TBL_LSG_REM(5) TBL_LSG_REM(6)
             TBL_LSG_REM(7)
 #undef TBL_LSG_REM
         }
     }
+    k_lsg_reduce<<<(2 * kit + 7) / 8, 256, 0, h->stream>>>(h->lsg_partial, h->red.max_blocks, nbd, kit, h->lsg_d,
+                                                            h->lsg_g);
     k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);  // kit <= 63
     int nbu = 6 * (h->n_sm > 0 ? h->n_sm : 148);  // one resident wave at 6 blocks per SM
     if (nbu > nb) nbu = nb;
     k_lsg_update_f<<<nbu, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
                                                       &hcol[kit]);
-    h->launches += 2 + (nfull > 0) + (rem > 0);
+    h->launches += 3 + (nfull > 0) + (rem > 0);
     return TBL_OK;
 }
 
