@@ -324,7 +324,9 @@ typedef struct {
  * tbl_backward_window, and return the window objective in *objective.  The
  * recycling means, Wt, new(k) and lamda must stay fixed over the window: a
  * window that would reach a rescaling step (every `cum` steps) is rejected
- * with TBL_ERR_BAD_ARG, as is a replay handle. */
+ * with TBL_ERR_BAD_ARG, as are a replay handle, the throughput-mode flags
+ * (red-black, span or streamwise SSOR blocks) and variants other than
+ * TBL_VARIANT_DNSTBL2. */
 int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* wc, double* objective,
                        tbl_step_stats* stats);
 

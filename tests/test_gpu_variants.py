@@ -98,3 +98,10 @@ def test_variant_rejections():
     g.upload(st)
     with pytest.raises(TblError):  # adjoint windows follow dnstbl2 only
         g.forward_window(2, 0.3, 1.5, 1)
+    rp.variant = abi.TBL_VARIANT_DNSTBL2
+    for flag in (abi.TBL_FLAG_SSOR_SPAN_BLOCKS, abi.TBL_FLAG_SSOR_STREAM_BLOCKS, abi.TBL_FLAG_RB_ORDER):
+        rp.flags = flag
+        g = TblGpu(mesh, rp)
+        g.upload(st)
+        with pytest.raises(TblError):  # and the reference's orderings and preconditioner
+            g.forward_window(2, 0.3, 1.5, 1)

@@ -930,8 +930,9 @@ int tbl_forward_window(tbl_handle* h, int32_t nsteps, const tbl_window_config* w
     if (!h || !wc || nsteps < 1 || wc->ckpt_every < 1) return TBL_ERR_BAD_ARG;
     if (wc->branch_mode < TBL_BRANCH_FREE || wc->branch_mode > TBL_BRANCH_REPLAY) return TBL_ERR_BAD_ARG;
     const tbl_config& c = h->cfg;
-    if (c.precision != TBL_PREC_FP64 || (c.flags & (TBL_FLAG_REPLAY | TBL_FLAG_RB_ORDER)) ||
-        c.variant != TBL_VARIANT_DNSTBL2)
+    const int32_t not_adjoint = TBL_FLAG_REPLAY | TBL_FLAG_RB_ORDER | TBL_FLAG_RB_PRECOND |
+                                TBL_FLAG_SSOR_SPAN_BLOCKS | TBL_FLAG_SSOR_STREAM_BLOCKS;
+    if (c.precision != TBL_PREC_FP64 || (c.flags & not_adjoint) || c.variant != TBL_VARIANT_DNSTBL2)
         return TBL_ERR_BAD_ARG;
     for (int s = 1; s <= nsteps; ++s)
         if ((h->cont + s) % c.cum == 0) return TBL_ERR_BAD_ARG;  // a rescaling step inside the window
