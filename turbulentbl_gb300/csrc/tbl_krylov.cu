@@ -42,22 +42,47 @@ __global__ void __launch_bounds__(RED_THREADS, 8) k_dot(long long n2, const doub
 // One modified Gram-Schmidt pass (:1140-1150):
 //   w -= (*hk) * vk          (skipped when vk == nullptr)
 //   *out = sum(vn * w)       (vn == nullptr: sum(w*w), op 1 takes the sqrt)
-__global__ void __launch_bounds__(RED_THREADS, 8) k_mgs(long long n2, double2* __restrict__ w,
-                                                     const double2* __restrict__ vk, const double* __restrict__ hk,
-                                                     const double2* __restrict__ vn, RedWork rw, int slot,
-                                                     double* out, int op) {
+// Two elements per thread per iteration with evict-first loads and stores
+// (the three vectors, 207 MB at 512x130x128, are far larger than L2), on a
+// grid of MGS_BLOCKS_PER_SM blocks per SM: 1.01 of the measured copy
+// bandwidth in a stand-alone copy, against 0.78 with one element, default
+// caching and 8 blocks per SM.
+constexpr int MGS_BLOCKS_PER_SM = 4;
+__global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __restrict__ w,
+                                                  const double2* __restrict__ vk, const double* __restrict__ hk,
+                                                  const double2* __restrict__ vn, RedWork rw, int slot, double* out,
+                                                  int op) {
     __shared__ double s_red[RED_THREADS / 32];
     const double hv = vk ? *hk : 0.0;
     double acc = 0.0;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2; q += (long long)gridDim.x * blockDim.x) {
-        double2 x = w[q];
+    const long long st = (long long)gridDim.x * blockDim.x;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; q + st < n2; q += 2 * st) {
+        double2 x0 = __ldcs(w + q), x1 = __ldcs(w + q + st);
         if (vk) {
-            double2 v = vk[q];
+            const double2 v0 = __ldcs(vk + q), v1 = __ldcs(vk + q + st);
+            x0.x = x0.x - hv * v0.x;
+            x0.y = x0.y - hv * v0.y;
+            x1.x = x1.x - hv * v1.x;
+            x1.y = x1.y - hv * v1.y;
+            __stcs(w + q, x0);
+            __stcs(w + q + st, x1);
+        }
+        const double2 y0 = vn ? __ldcs(vn + q) : x0, y1 = vn ? __ldcs(vn + q + st) : x1;
+        acc += y0.x * x0.x;
+        acc += y0.y * x0.y;
+        acc += y1.x * x1.x;
+        acc += y1.y * x1.y;
+    }
+    if (q < n2) {
+        double2 x = __ldcs(w + q);
+        if (vk) {
+            const double2 v = __ldcs(vk + q);
             x.x = x.x - hv * v.x;
             x.y = x.y - hv * v.y;
-            w[q] = x;
+            __stcs(w + q, x);
         }
-        double2 y = vn ? vn[q] : x;
+        const double2 y = vn ? __ldcs(vn + q) : x;
         acc += y.x * x.x;
         acc += y.y * x.y;
     }
@@ -262,7 +287,8 @@ int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int
 }
 
 int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op) {
-    int nb = red_blocks(h);
+    int nb = MGS_BLOCKS_PER_SM * (h->n_sm > 0 ? h->n_sm : 148);
+    if (nb > red_blocks(h)) nb = red_blocks(h);
     k_mgs<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, (const double2*)vk, hk, (const double2*)vn,
                                              h->red, 7, out, op);
     h->launches++;
