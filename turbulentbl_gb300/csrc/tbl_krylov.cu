@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
         const float4 x = w[q], l = vl[q];
 #pragma unroll
         for (int e = 0; e < G; ++e) {
-            const float4 v = V[(long long)(i0 + e) * vstride4 + q];
+            const float4 v = __ldcs(V + (long long)(i0 + e) * vstride4 + q);  // read once: evict first
             fd[e] += dot4f(v, x);
             fg[e] += dot4f(v, l);
         }
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(RED_THREADS, 6) k_lsg_update_f(long long n4, f
         float4 x = w[q];
 #pragma unroll 4
         for (int i = 0; i < nv; ++i) {
-            const float4 v = V[(long long)i * vstride4 + q];
+            const float4 v = __ldcs(V + (long long)i * vstride4 + q);  // read once: evict first
             const float ti = s_t[i];
             x.x = fmaf(-ti, v.x, x.x);
             x.y = fmaf(-ti, v.y, x.y);
