@@ -333,12 +333,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
 #pragma unroll
                     for (int e = CH - 1; e >= 0; --e) { carry = fma(ci, carry, nv[e]); nv[e] = carry; }
                 }
-#pragma unroll
-                for (int e = 0; e < CH; ++e) outp[i0 + e] = nv[e];
-                if (MODE == SW_GS && hout) {
-#pragma unroll
-                    for (int e = 0; e < CH; ++e) hout[i0 + e] = nv[e];
-                }
             } else {  // first / last chunk: points outside 1..nx-2 are boundary values or zero
                 if (MODE != SW_BWD) {
                     Val prev = c == 0 ? (MODE == SW_GS ? cbnd : Val(0)) : carry;
@@ -359,12 +353,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
                     }
                     carry = prev;
                 }
-#pragma unroll
-                for (int e = 0; e < CH; ++e) {
-                    const int i = i0 + e;
-                    if (MODE != SW_GS || (i >= 1 && i <= g.nx - 2)) outp[i0 + e] = nv[e];
-                    if (MODE == SW_GS && hout && i >= 1 && i <= g.nx - 2) hout[i0 + e] = nv[e];
-                }
             }
 #pragma unroll
             for (int e = 0; e < CH; ++e) last[e] = nv[e];
@@ -383,9 +371,24 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             for (int e = 0; e < CH; ++e) ws[e] = last[e];
         }
         __syncwarp();
-        if (lane == 0) {
-            st_release_cta(&s_prog[wid], T);
-            if ((T - T0) % PUB == PUB - 1 || T == T1) st_release(fme, tag + (unsigned long long)(T + 1));
+        if (lane == 0) st_release_cta(&s_prog[wid], T);
+        // the results go to global memory after the hand-off to the next
+        // plane, which reads the ring only, so that release does not wait for
+        // these stores; the device-scope progress flag (for the CTAs that
+        // read the rows and planes from global memory) is released after them
+        if (act) {
+            const bool all = !edge || MODE != SW_GS;
+#pragma unroll
+            for (int e = 0; e < CH; ++e) {
+                const int i = i0 + e;
+                const bool in = all || (i >= 1 && i <= g.nx - 2);
+                if (in) outp[i0 + e] = last[e];
+                if (MODE == SW_GS && hout && (edge ? (i >= 1 && i <= g.nx - 2) : true)) hout[i0 + e] = last[e];
+            }
+        }
+        if ((T - T0) % PUB == PUB - 1 || T == T1) {
+            __syncwarp();
+            if (lane == 0) st_release(fme, tag + (unsigned long long)(T + 1));
         }
         // ---- cross-CTA inputs of step T+1 when their producer is known to be ahead
         pj_ok = false;
