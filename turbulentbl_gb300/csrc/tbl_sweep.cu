@@ -422,6 +422,8 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
 // FMA order: PRE = fma(p3, U(k+1), fma(p2, U(j+1), fma(p1, U(i+1), p0 Q))).
 // Fully parallel, so the wavefront sweep keeps only the three FMAs that
 // depend on new values.  blockIdx.z runs over (component, plane).
+constexpr int ROWS_PER_BLOCK = 4;  // span rows per block of the fully parallel per-point passes
+
 template <typename T>
 struct Ptr3 {
     const T* p[3];
@@ -455,24 +457,27 @@ __global__ void __launch_bounds__(256) k_gs_pre(Geom g, const T* __restrict__ pc
                                                 Ptr3<T> Fs, Ptr3<T> Qs, Ptr3<T> PREs,
                                                 const T* __restrict__ halo_in) {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y;
     const int K = g.nz - 2;
     const int ci = blockIdx.z / K, k = 1 + blockIdx.z % K;
     if (i > g.nx - 2) return;
     const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
     const T* F = Fs.p[comp];
-    const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
     const int nz = g.nz;
     const T p0 = pc[k], p1 = pc[nz + k], p2 = pc[2 * nz + k], p3 = pc[3 * nz + k];
-    const int jp = (j == g.ny - 2) ? 1 : j + 1;
     const int r = slab_of_k[k];
     const SlabDesc sl = slabs[r];
-    const T* Fkp = (k == sl.bn + sl.K - 1 && r < P - 1)
-                       ? halo_in + ((size_t)comp * 2 * P + 1 * P + r) * (size_t)g.ps + (size_t)g.sx * j
-                       : F + line + g.ps;
-    T x = fma(p1, F[line + i + 1], p0 * Qs.p[comp][line + i]);
-    if (jp != 1) x = fma(p2, F[(long long)g.sx * ((long long)jp + (long long)g.ny * k) + i], x);
-    const_cast<T*>(PREs.p[comp])[line + i] = fma(p3, Fkp[i], x);
+    const bool halo = k == sl.bn + sl.K - 1 && r < P - 1;
+    for (int jr = 0; jr < ROWS_PER_BLOCK; ++jr) {  // a few rows per block: fewer, longer blocks
+        const int j = 1 + blockIdx.y * ROWS_PER_BLOCK + jr;
+        if (j > g.ny - 2) break;
+        const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
+        const int jp = (j == g.ny - 2) ? 1 : j + 1;
+        const T* Fkp = halo ? halo_in + ((size_t)comp * 2 * P + 1 * P + r) * (size_t)g.ps + (size_t)g.sx * j
+                            : F + line + g.ps;
+        T x = fma(p1, F[line + i + 1], p0 * Qs.p[comp][line + i]);
+        if (jp != 1) x = fma(p2, F[(long long)g.sx * ((long long)jp + (long long)g.ny * k) + i], x);
+        const_cast<T*>(PREs.p[comp])[line + i] = fma(p3, Fkp[i], x);
+    }
 }
 
 // ------------------------------ red-black ordering (TBL_FLAG_RB_ORDER)
@@ -495,21 +500,25 @@ __device__ __forceinline__ int rb_i0(int color, int j, int k) { return 2 - ((col
 template <typename T>
 __global__ void __launch_bounds__(256) k_rb_gs(Geom g, const T* __restrict__ pc, const T* __restrict__ pbv,
                                                Ptr3<T> Fs, Ptr3<T> Qs, int c0_, int c1_, int c2_, int color) {
-    const int j = 1 + blockIdx.y;
     const int K = g.nz - 2;
     const int ci = blockIdx.z / K, k = 1 + blockIdx.z % K;
-    const int i = rb_i0(color, j, k) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (i > g.nx - 2) return;
     const int comp = ci == 0 ? c0_ : (ci == 1 ? c1_ : c2_);
     T* F = const_cast<T*>(Fs.p[comp]);
+    const T* Q = Qs.p[comp];
     const int nz = g.nz;
     const T p0 = pc[k], p1 = pc[nz + k], p2 = pc[2 * nz + k], p3 = pc[3 * nz + k], pb = pbv[k];
-    const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
-    const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
-    const long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
-    const long long pjp = (long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k);
-    F[p] = p0 * Qs.p[comp][p] + p1 * (F[p + 1] + F[p - 1]) + p2 * (F[pjp] + F[pjm]) + p3 * F[p + g.ps] +
-           pb * F[p - g.ps];
+    for (int jr = 0; jr < ROWS_PER_BLOCK; ++jr) {  // a few rows per block: fewer, longer blocks
+        const int j = 1 + blockIdx.y * ROWS_PER_BLOCK + jr;
+        if (j > g.ny - 2) break;
+        const int i = rb_i0(color, j, k) + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+        if (i > g.nx - 2) continue;
+        const int jm = j == 1 ? g.ny - 2 : j - 1, jp = j == g.ny - 2 ? 1 : j + 1;
+        const long long p = (long long)i + (long long)g.sx * ((long long)j + (long long)g.ny * k);
+        const long long pjm = (long long)i + (long long)g.sx * ((long long)jm + (long long)g.ny * k);
+        const long long pjp = (long long)i + (long long)g.sx * ((long long)jp + (long long)g.ny * k);
+        F[p] = p0 * Q[p] + p1 * (F[p + 1] + F[p - 1]) + p2 * (F[pjp] + F[pjm]) + p3 * F[p + g.ps] +
+               pb * F[p - g.ps];
+    }
 }
 
 // Red-black SSOR preconditioner (one global block, periodic in j), the same
@@ -685,7 +694,7 @@ static int gs_pre_and_sweep(tbl_handle* h, T* const F[3], const T* const Q[3], T
     const Geom& g = h->g;
     Ptr3<T> Fs, Qs, Ps;
     for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; Ps.p[c] = PRE[c]; }
-    dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
+    dim3 grid((g.nx - 2 + 255) / 256, (g.ny - 2 + ROWS_PER_BLOCK - 1) / ROWS_PER_BLOCK, (g.nz - 2) * ncomp);
     const T* pc = sizeof(T) == 8 ? (const T*)h->gs_coef : (const T*)h->gs_coef_f;
     k_gs_pre<T><<<grid, 256, 0, h->stream>>>(g, pc, h->slab_of_k, h->slabs, h->P,
                                              comps[0], ncomp > 1 ? comps[1] : 0, ncomp > 2 ? comps[2] : 0, Fs, Qs,
@@ -705,7 +714,7 @@ static int rb_gs(tbl_handle* h, T* const F[3], const T* const Q[3], const T* pc,
     const Geom& g = h->g;
     Ptr3<T> Fs, Qs;
     for (int c = 0; c < 3; ++c) { Fs.p[c] = F[c]; Qs.p[c] = Q[c]; }
-    dim3 grid(((g.nx - 1) / 2 + 255) / 256, g.ny - 2, (g.nz - 2) * ncomp);
+    dim3 grid(((g.nx - 1) / 2 + 255) / 256, (g.ny - 2 + ROWS_PER_BLOCK - 1) / ROWS_PER_BLOCK, (g.nz - 2) * ncomp);
     for (int color = 0; color < 2; ++color)
         k_rb_gs<T><<<grid, 256, 0, h->stream>>>(g, pc, pb, Fs, Qs, comps[0], ncomp > 1 ? comps[1] : 0,
                                                 ncomp > 2 ? comps[2] : 0, color);
