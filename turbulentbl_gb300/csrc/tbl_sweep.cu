@@ -132,10 +132,11 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 //   FWD: x = w'*r + w'*As*x(j-1) + w'*Ab*x(k-1) + w'*Aw*x(i-1),   w' = -w/Ap
 //   BWD: y = w'*s*rhat + w'*As*y(j+1) + w'*At*y(k+1) + w'*Aw*y(i+1)
 // which changes only the rounding of the reference's left-to-right sums.
-// Operands of step T+1 that do not depend on other lines are loaded while
-// step T runs; the (k-1) values of the plane below come through a shared
-// memory ring (RING steps deep, with back-pressure), the (j-1) values of the
-// row above by shuffle or, for lane 0, from global memory.
+// Operands of step T that do not depend on other lines are loaded at the
+// start of the step, while the warp waits for its producers; the (k-1) values
+// of the plane below come through a shared memory ring (RING steps deep, with
+// back-pressure), the (j-1) values of the row above by shuffle or, for lane
+// 0, from global memory.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     Val carry = Val(0);
     long long seen_j = -1, seen_k = -1;
 
-    // raw operands loaded one step ahead
+    // raw operands, loaded at the start of their step
     Val ra[CH];
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
@@ -260,8 +261,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
 #pragma unroll
         for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
     };
-    load_raw(T0);
-    make_pre(T0);
     const Val bnd = MODE == SW_GS ? F[0] : Val(0);  // GS: U(0), the inflow boundary value of the line
     Val pj_pf[CH], pk_pf[CH];
     bool pj_ok = false, pk_ok = false;
@@ -274,11 +273,12 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         const int i0 = CH * c;
         const bool edge = (c == 0) || (c == C - 1);
         if (cl == 0) carry = Val(0);  // first chunk of the line in this block: nothing before it
-        Val cur[CH];
-#pragma unroll
-        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
         const Val cbnd = bnd;
-        load_raw(T + 1);
+        // this step's operands, in flight while the warp waits for its
+        // producers.  Loading them a step ahead instead was slower (FP64 SSOR
+        // sweeps 295 -> 273 ms per box512 step without it): loads still in
+        // flight at the end-of-step release have to complete first.
+        load_raw(T);
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
         if (lane == 0) {
             const int cl0 = T - (32 * cta.jb - jblk0) - kl;
@@ -297,6 +297,10 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             }
         }
         __syncwarp();
+        make_pre(T);
+        Val cur[CH];
+#pragma unroll
+        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
         // ---- predecessors
         Val pj[CH], pk[CH];
 #pragma unroll
@@ -411,7 +415,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
                 pk_ok = pf != 0;
             }
         }
-        make_pre(T + 1);
     }
     (void)tend_j;
 }
