@@ -133,7 +133,7 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 //   BWD: y = w'*s*rhat + w'*As*y(j+1) + w'*At*y(k+1) + w'*Aw*y(i+1)
 // which changes only the rounding of the reference's left-to-right sums.
 // Operands of step T that do not depend on other lines are loaded at the
-// start of the step, while the warp waits for its producers; the (k-1) values
+// start of the step, before the warp waits for its producers; the (k-1) values
 // of the plane below come through a shared memory ring (RING steps deep, with
 // back-pressure), the (j-1) values of the row above by shuffle or, for lane
 // 0, from global memory.
@@ -274,11 +274,16 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         const bool edge = (c == 0) || (c == C - 1);
         if (cl == 0) carry = Val(0);  // first chunk of the line in this block: nothing before it
         const Val cbnd = bnd;
-        // this step's operands, in flight while the warp waits for its
-        // producers.  Loading them a step ahead instead was slower (FP64 SSOR
-        // sweeps 295 -> 273 ms per box512 step without it): loads still in
-        // flight at the end-of-step release have to complete first.
+        // this step's operands, loaded and scaled before the warp waits for
+        // its producers.  Loading them a step ahead instead was slower (FP64
+        // SSOR sweeps 295 -> 273 ms per box512 step without it): loads still
+        // in flight at the end-of-step release have to complete first; and
+        // scaling them after the wait puts the BWD multiply on the chain.
         load_raw(T);
+        make_pre(T);
+        Val cur[CH];
+#pragma unroll
+        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
         if (lane == 0) {
             const int cl0 = T - (32 * cta.jb - jblk0) - kl;
@@ -297,10 +302,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             }
         }
         __syncwarp();
-        make_pre(T);
-        Val cur[CH];
-#pragma unroll
-        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
         // ---- predecessors
         Val pj[CH], pk[CH];
 #pragma unroll
@@ -376,10 +377,16 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         }
         __syncwarp();
         if (lane == 0) st_release_cta(&s_prog[wid], T);
-        // the results go to global memory after the hand-off to the next
+        // The results go to global memory after the hand-off to the next
         // plane, which reads the ring only, so that release does not wait for
-        // these stores; the device-scope progress flag (for the CTAs that
-        // read the rows and planes from global memory) is released after them
+        // these stores.  The device-scope progress flag (for the CTAs that
+        // read rows and planes from global memory) publishes the previous
+        // step before this step's stores, whose completion it would
+        // otherwise wait for; the last step is published after its stores.
+        if (T > T0 && (T - T0) % PUB == 0) {
+            __syncwarp();
+            if (lane == 0) st_release(fme, tag + (unsigned long long)T);  // steps up to T-1 done
+        }
         if (act) {
             const bool all = !edge || MODE != SW_GS;
 #pragma unroll
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
                 if (MODE == SW_GS && hout && (edge ? (i >= 1 && i <= g.nx - 2) : true)) hout[i0 + e] = last[e];
             }
         }
-        if ((T - T0) % PUB == PUB - 1 || T == T1) {
+        if (T == T1) {
             __syncwarp();
             if (lane == 0) st_release(fme, tag + (unsigned long long)(T + 1));
         }
