@@ -377,16 +377,10 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         }
         __syncwarp();
         if (lane == 0) st_release_cta(&s_prog[wid], T);
-        // The results go to global memory after the hand-off to the next
+        // the results go to global memory after the hand-off to the next
         // plane, which reads the ring only, so that release does not wait for
-        // these stores.  The device-scope progress flag (for the CTAs that
-        // read rows and planes from global memory) publishes the previous
-        // step before this step's stores, whose completion it would
-        // otherwise wait for; the last step is published after its stores.
-        if (T > T0 && (T - T0) % PUB == 0) {
-            __syncwarp();
-            if (lane == 0) st_release(fme, tag + (unsigned long long)T);  // steps up to T-1 done
-        }
+        // these stores; the device-scope progress flag (for the CTAs that
+        // read the rows and planes from global memory) is released after them
         if (act) {
             const bool all = !edge || MODE != SW_GS;
 #pragma unroll
@@ -397,7 +391,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
                 if (MODE == SW_GS && hout && (edge ? (i >= 1 && i <= g.nx - 2) : true)) hout[i0 + e] = last[e];
             }
         }
-        if (T == T1) {
+        if ((T - T0) % PUB == PUB - 1 || T == T1) {
             __syncwarp();
             if (lane == 0) st_release(fme, tag + (unsigned long long)(T + 1));
         }
