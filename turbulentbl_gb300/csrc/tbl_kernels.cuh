@@ -41,7 +41,6 @@ int launch_restart_init(tbl_handle* h, int first);
 int launch_ppe_resid(tbl_handle* h);
 int red_blocks(tbl_handle* h);
 int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int op);
-int launch_mgs_f(tbl_handle* h, float* w, const float* vk, const double* hk, const float* vn, double* out, int op);
 int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom);
 int launch_backsub_update_f(tbl_handle* h, int kit);
 int launch_restart_init_k(tbl_handle* h, int first, int K1);

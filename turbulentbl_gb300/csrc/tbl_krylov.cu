@@ -227,28 +227,6 @@ __global__ void __launch_bounds__(RED_THREADS, 8) k_dot_f(long long n4, const fl
     grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
 }
 
-__global__ void __launch_bounds__(RED_THREADS, 8) k_mgs_f(long long n4, float4* __restrict__ w,
-                                                       const float4* __restrict__ vk, const double* __restrict__ hk,
-                                                       const float4* __restrict__ vn, RedWork rw, int slot,
-                                                       double* out, int op) {
-    __shared__ double s_red[RED_THREADS / 32];
-    const float hv = vk ? (float)*hk : 0.0f;
-    double acc = 0.0;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
-        float4 x = w[q];
-        if (vk) {
-            float4 v = vk[q];
-            x.x = fmaf(-hv, v.x, x.x);
-            x.y = fmaf(-hv, v.y, x.y);
-            x.z = fmaf(-hv, v.z, x.z);
-            x.w = fmaf(-hv, v.w, x.w);
-            w[q] = x;
-        }
-        acc += dot4(vn ? vn[q] : x, x);
-    }
-    double bt = block_sum(acc, s_red);
-    grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
-}
 
 __global__ void k_scale_inv_f(long long n4, float4* __restrict__ w, const double* __restrict__ denom) {
     const double d = *denom;
@@ -510,14 +488,6 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
 int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int op) {
     int nb = red_blocks(h);
     k_dot_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (const float4*)a, (const float4*)b, h->red, 7, out, op);
-    h->launches++;
-    return TBL_OK;
-}
-
-int launch_mgs_f(tbl_handle* h, float* w, const float* vk, const double* hk, const float* vn, double* out, int op) {
-    int nb = red_blocks(h);
-    k_mgs_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (float4*)w, (const float4*)vk, hk, (const float4*)vn,
-                                               h->red, 7, out, op);
     h->launches++;
     return TBL_OK;
 }

@@ -126,7 +126,7 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 //
 // Per step a lane updates CH points of its line.  The point update is
 // reassociated so that only one FMA depends on the previous point:
-//   GS : x = rd*Q - rd*cE*U(i+1) - rd*cN*U(j+1) - rd*cT*U(k+1)       (prefetch)
+//   GS : x = rd*Q - rd*cE*U(i+1) - rd*cN*U(j+1) - rd*cT*U(k+1)       (k_gs_pre)
 //            - rd*cS*x(j-1) - rd*cB*x(k-1)                            (after wait)
 //            - rd*cW*x(i-1)                                           (chain)
 //   FWD: x = w'*r + w'*As*x(j-1) + w'*Ab*x(k-1) + w'*Aw*x(i-1),   w' = -w/Ap
