@@ -250,9 +250,11 @@ __global__ void k_update_f(long long n4, double* __restrict__ pc, const float4* 
             const float y = (float)gy[i];
             c.x = fmaf(y, v.x, c.x); c.y = fmaf(y, v.y, c.y); c.z = fmaf(y, v.z, c.z); c.w = fmaf(y, v.w, c.w);
         }
-        double4 x = reinterpret_cast<double4*>(pc)[q];
-        x.x += (double)c.x; x.y += (double)c.y; x.z += (double)c.z; x.w += (double)c.w;
-        reinterpret_cast<double4*>(pc)[q] = x;
+        double2* p2 = reinterpret_cast<double2*>(pc) + 2 * q;
+        double2 x0 = p2[0], x1 = p2[1];
+        x0.x += (double)c.x; x0.y += (double)c.y; x1.x += (double)c.z; x1.y += (double)c.w;
+        p2[0] = x0;
+        p2[1] = x1;
     }
 }
 

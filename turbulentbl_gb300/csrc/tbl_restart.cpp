@@ -36,7 +36,7 @@ bool valid_format(int f) { return f == TBL_TP_DNSTBL2 || f == TBL_TP_ORIGINAL ||
 // the exponent is one more than C's (mantissa 0.d... instead of d.d...).  An
 // exponent beyond two digits drops the E, as Ew.d does.
 void put_e(std::string& out, double v) {
-    char buf[64], body[64];
+    char buf[64], body[40];
     if (v == 0.0) {
         snprintf(body, sizeof body, "0.000000000000000E+00");
     } else if (!std::isfinite(v)) {
@@ -55,8 +55,9 @@ void put_e(std::string& out, double v) {
         else
             snprintf(body, sizeof body, "%s0.%sE%c%02d", sg, digits, ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
     }
-    snprintf(buf, sizeof buf, " %22s", body);
-    out += buf;
+    char field[64];
+    snprintf(field, sizeof field, " %22s", body);
+    out += field;
 }
 
 void put_f(std::string& out, double v, int w, int d) {
