@@ -86,7 +86,7 @@ def case():
     ct = _full(c, mesh.ny).requires_grad_(True)
     Jt, _, _ = _torch_window(ts, x0, ct, W)
     (gt,) = torch.autograd.grad(Jt, ct)
-    return dict(mesh=mesh, rp=rp, g=g, x0=x0, c=c, ts=ts, Jt=float(Jt), gt=gt[:, 1:mesh.ny - 1].numpy())
+    return dict(mesh=mesh, rp=rp, g=g, x0=x0, c=c, ts=ts, Jt=float(Jt.detach()), gt=gt[:, 1:mesh.ny - 1].numpy())
 
 
 def test_window_objective_and_gradient_match_autograd(case):
