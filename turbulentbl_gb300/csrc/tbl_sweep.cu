@@ -98,6 +98,18 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
 }
 
 constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
+constexpr int NPF = 3;   // operand slots per warp: a step's operands are copied two steps ahead
+
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only), its group
+// commit and the wait for all but the most recent N groups.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 constexpr int PUB = 4;   // global progress is published every PUB steps (and at the end)
 
 __device__ __forceinline__ int ld_acquire_cta(const int* p) {
@@ -159,6 +171,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
     __shared__ int s_prog[KG];
     __shared__ __align__(16) Val s_ring[KG][RING][32][CH];
+    __shared__ __align__(16) Val s_pf[KG][NPF][32][CH];
     if (lane == 0) s_prog[wid] = -1;
     __syncthreads();
 
@@ -243,16 +256,31 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     Val carry = Val(0);
     long long seen_j = -1, seen_k = -1;
 
-    // raw operands, loaded at the start of their step
-    Val ra[CH];
+    // raw operands.  Each lane copies its own 32 bytes (FP64) or 16 bytes
+    // (FP32) of step ts's operands into its shared-memory slot two steps
+    // ahead with cp.async (one commit group per step, empty when the lane
+    // has nothing to load) and waits for that group at the top of step ts.
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
+    Val ra[CH];
+    auto issue_raw = [&](int ts) {
+        const int cl = ts - jr - kl;
+        if (line_ok && ts <= T1 && cl >= 0 && cl < Cl) {
+            const int i0 = CH * (MODE == SW_BWD ? c_hi - cl : c_lo + cl);
+            Val* dst = &s_pf[wid][ts % NPF][lane][0];
+#pragma unroll
+            for (int b = 0; b < (int)(CH * sizeof(Val)) / 16; ++b)
+                cp_async16(dst + b * (16 / sizeof(Val)), inp + i0 + b * (16 / sizeof(Val)));
+        }
+        cp_async_commit();
+    };
     auto load_raw = [&](int ts) {
         const int cl = ts - jr - kl;
+        cp_async_wait<1>();  // all but the group of step ts + 1
         if (!line_ok || cl < 0 || cl >= Cl) return;
-        const int i0 = CH * (MODE == SW_BWD ? c_hi - cl : c_lo + cl);
+        const Val* src = &s_pf[wid][ts % NPF][lane][0];
 #pragma unroll
-        for (int e = 0; e < CH; ++e) ra[e] = inp[i0 + e];
+        for (int e = 0; e < CH; ++e) ra[e] = src[e];
     };
     Val pre[CH];
     auto make_pre = [&](int ts) {
@@ -262,6 +290,8 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
     };
     const Val bnd = MODE == SW_GS ? F[0] : Val(0);  // GS: U(0), the inflow boundary value of the line
+    issue_raw(T0);
+    issue_raw(T0 + 1);
     Val pj_pf[CH], pk_pf[CH];
     bool pj_ok = false, pk_ok = false;
     int abort = 0;
@@ -274,11 +304,12 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         const bool edge = (c == 0) || (c == C - 1);
         if (cl == 0) carry = Val(0);  // first chunk of the line in this block: nothing before it
         const Val cbnd = bnd;
-        // this step's operands, loaded and scaled before the warp waits for
-        // its producers.  Loading them a step ahead instead was slower (FP64
-        // SSOR sweeps 295 -> 273 ms per box512 step without it): loads still
-        // in flight at the end-of-step release have to complete first; and
-        // scaling them after the wait puts the BWD multiply on the chain.
+        // this step's operands, read from the shared-memory slot and scaled
+        // before the warp waits for its producers.  A register prefetch a
+        // step ahead was slower (loads still in flight at the end-of-step
+        // release have to complete first); cp.async copies are not ordered
+        // by that release, so they run two steps ahead (box512 FP64 SSOR
+        // sweeps 284 -> 256 ms per step, GS 83 -> 79 ms).
         load_raw(T);
         make_pre(T);
         Val cur[CH];
@@ -308,6 +339,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         for (int e = 0; e < CH; ++e) pj[e] = __shfl_up_sync(0xffffffffu, last[e], 1);
         if (__shfl_sync(0xffffffffu, abort, 0)) {
             if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
+            cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
             return;
         }
         if (act) {
@@ -369,6 +401,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             __syncwarp();
             if (__shfl_sync(0xffffffffu, abort, 0)) {
                 if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
+                cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
                 return;
             }
             Val* ws = &s_ring[wid][T & (RING - 1)][lane][0];
@@ -416,7 +449,9 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
                 pk_ok = pf != 0;
             }
         }
+        issue_raw(T + 2);
     }
+    cp_async_wait<0>();
     (void)tend_j;
 }
 
