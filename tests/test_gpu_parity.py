@@ -38,8 +38,13 @@ def compare(o, g, fields=("u", "v", "w", "p", "pcorr")):
     return {f: rel(b[f], a[f]) for f in fields}, a, b
 
 
-@pytest.mark.parametrize("nx,nzs,nyw,P", [(24, 12, 20, 2), (30, 10, 26, 3), (21, 7, 17, 1), (40, 34, 33, 4)])
+@pytest.mark.parametrize("nx,nzs,nyw,P", [(24, 12, 20, 2), (30, 10, 26, 3), (21, 7, 17, 1), (40, 34, 33, 4),
+                                          (20, 4, 16, 2), (22, 5, 16, 2), (26, 70, 12, 2)])
 def test_free_running_steps_match(nx, nzs, nyw, P):
+    """Grids with 4 span rows or fewer sweep with a row lag of a whole chunk
+    (the Gauss-Seidel wrap row would otherwise share a step with row 1); 5
+    rows is the smallest grid with the one-position lag; 70 rows span three
+    32-row blocks."""
     o, g, _ = pair(nx, nzs, nyw, P)
     for s in range(7):
         so, _ = o.step(1, check=False)

@@ -8,12 +8,14 @@
 // (k+1), so any schedule that respects that partial order performs exactly
 // the same arithmetic per point.  The schedule used here:
 //
-//   * every (j,k) line of a slab is owned by one lane; a lane walks its line
-//     in chunks of CHUNK=4 consecutive i (one 32-byte sector);
-//   * line (j,k) processes chunk c at logical step T = c + j + k, so its
-//     (j-1) and (k-1) predecessors finished chunk c at step T-1;
-//   * a warp holds 32 consecutive rows of one plane (the j-1 value comes from
-//     the neighbouring lane by shuffle); a CTA holds KG planes;
+//   * every (j,k) line of a slab is owned by one lane; a lane updates
+//     CHUNK=4 consecutive points of its line per step;
+//   * a warp holds 32 consecutive rows of one plane, a CTA holds KG planes;
+//     point i of row j is updated one position after point i of row j-1 (the
+//     value comes from the neighbouring lane by shuffle, within the step or
+//     from the step before) and one step after point i of plane k-1 (through
+//     shared memory), so a sweep takes about nx/4 + K + 9 (ny-2)/32 steps
+//     instead of the nx/4 + K + (ny-2) of a chunk-per-row lag;
 //   * every warp waits only for the warps producing its inputs: the warp of
 //     the row block above (global progress flag, acquire/release) and the
 //     warp of the plane below (shared-memory progress inside the CTA, a
@@ -56,6 +58,7 @@ struct SweepArgs {
     double omega, sw;           // w, (2-w)/w
     int jb_rows;                // SSOR: rows per span block (a multiple of 32; 0 = one block per slab)
     int nib;                    // SSOR: streamwise blocks (grid.y), 1 = one block per line
+    int plag;                   // positions a row lags the row above: 1, or CHUNK (see base_args)
     const T* X;                 // matvec input (FWD) / PCorr (FWD residual mode)
     const double* Q8;           // residual mode when non-null
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
@@ -98,7 +101,8 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
 }
 
 constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
-constexpr int NPF = 3;   // operand slots per warp: a step's operands are copied two steps ahead
+constexpr int NPF = 4;   // operand slots per warp: chunks are copied two steps ahead, and a slot is
+                         // rewritten one step after its last read
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only), its group
 // commit and the wait for all but the most recent N groups.
@@ -149,9 +153,12 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // of the plane below come through a shared memory ring (RING steps deep, with
 // back-pressure), the (j-1) values of the row above by shuffle or, for lane
 // 0, from global memory.
+// FP32 sweeps keep 6 CTAs per SM (80 registers), FP64 ones 4, so that the Gauss-Seidel
+// sweeps of two velocity components stay co-resident on large grids.
 template <int MODE, typename Val>
-__global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
+__global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(SweepArgs<Val> a) {
     constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
+    static_assert(CH == CHUNK && CH == 4, "positions map to chunks by shifts");
     const Geom& g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const SweepCta cta = a.ctas[blockIdx.x];
@@ -180,6 +187,7 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     // jb_rows rows (the row before a block reads zero, as across slabs)
     const int jblk0 = (MODE != SW_GS && a.jb_rows > 0) ? (32 * cta.jb / a.jb_rows) * a.jb_rows : 0;
     const int jr = jl - jblk0;          // row within its span block
+    const int bj = (32 * cta.jb - jblk0) >> 5;  // 32-row block of this warp within the span block
     const int kl = KG * cta.kg + wid;   // logical plane
     if (kl >= K) return;                // no lines: nobody waits for this warp
     const bool line_ok = jl < J;
@@ -191,17 +199,32 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     const long long line = (long long)g.sx * ((long long)j + (long long)g.ny * k);
     const long long sy = g.sx;
 
-    const int jl_last = min(32 * cta.jb + 31, J - 1) - jblk0;  // within the span block
-    const int T0 = 32 * cta.jb - jblk0 + kl;
-    const int T1 = jl_last + kl + Cl - 1;
+    // Schedule.  The block's positions along a line are q = 0 .. Q-1 in sweep
+    // order (i = CH*c_lo + q, or CH*c_hi + CH-1 - q backwards).  Lane l of
+    // this warp updates positions q = CH*(T - T0) - plag*l + e, e = 0..CH-1,
+    // at step T: a row lags the row above by plag positions (its (j-1) input
+    // at the same q is the neighbour lane's point e - plag of this step, or of
+    // the step before), the plane above lags by one step (its (k-1) input is
+    // the same lane's point e of the plane below one step earlier), and a
+    // 32-row block lags the block above by blag steps, the least that puts
+    // its row-above inputs in the block above's completed steps.
+    const int plag = a.plag;
+    const int blag = (31 * plag + 2 * CH - 1) / CH;
+    const int lane_last = min(32 * cta.jb + 31, J - 1) - 32 * cta.jb;  // last row of the warp
+    const int Q = CH * Cl;
+    const int T0 = kl + blag * bj;                              // lane 0's first step
+    const int T1 = T0 + (Q - 1 + plag * lane_last) / CH;        // the last row's last step
     const int tend_k = T1 - 1;          // last step of the (k-1) upstream warp
-    const int tend_j = 32 * cta.jb - jblk0 - 1 + kl + Cl - 1;
+    const int dl = plag * lane;         // this lane's lag in positions
     const bool has_down = wid < KG - 1 && kl + 1 < K;
     const unsigned long long* fj =
         (cta.up_j >= 0 && 32 * cta.jb != jblk0) ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
     const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
     unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
     const unsigned long long tag = a.epoch << 20;
+    // physical i of position q
+    const int ibase = MODE == SW_BWD ? CH * c_hi + CH - 1 : CH * c_lo;
+    const int idir = MODE == SW_BWD ? -1 : 1;
 
     // coefficients of this plane, pre-scaled for the reassociated update (FP64)
     double c0 = 0, c1 = 0, c2 = 0, c3 = 0, cjd = 0, ckd = 0, cid = 0;
@@ -250,44 +273,32 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     const Val* inp = MODE == SW_GS ? a.PRE[comp] + line : a.RH + line;
     const bool wrap = MODE == SW_GS && jp == 1;  // the row after j holds new values (periodic GS)
 
-    Val last[CH];
+    Val last[CH];  // this lane's outputs of the previous step
 #pragma unroll
     for (int e = 0; e < CH; ++e) last[e] = Val(0);
     Val carry = Val(0);
     long long seen_j = -1, seen_k = -1;
 
-    // raw operands.  Each lane copies its own 32 bytes (FP64) or 16 bytes
-    // (FP32) of step ts's operands into its shared-memory slot two steps
-    // ahead with cp.async (one commit group per step, empty when the lane
-    // has nothing to load) and waits for that group at the top of step ts.
+    // raw operands.  The lane's window of step ts ends in chunk
+    // a(ts) = (CH*(ts - T0) - dl + CH-1) / CH of the block (floor); each lane
+    // copies that chunk (32 bytes FP64, 16 bytes FP32) into its shared-memory
+    // slot ts % NPF two steps ahead with cp.async (one commit group per step,
+    // empty when the chunk is outside the block or the lane has no line) and
+    // waits for the group at the top of step ts.  A window that is not
+    // chunk-aligned also reads the previous chunk, still in slot (ts-1) % NPF.
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
-    Val ra[CH];
+    auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };
     auto issue_raw = [&](int ts) {
-        const int cl = ts - jr - kl;
-        if (line_ok && ts <= T1 && cl >= 0 && cl < Cl) {
-            const int i0 = CH * (MODE == SW_BWD ? c_hi - cl : c_lo + cl);
+        const int ac = chunk_of(ts);
+        if (line_ok && ts <= T1 && ac >= 0 && ac < Cl) {
+            const int i0 = CH * (MODE == SW_BWD ? c_hi - ac : c_lo + ac);
             Val* dst = &s_pf[wid][ts % NPF][lane][0];
 #pragma unroll
             for (int b = 0; b < (int)(CH * sizeof(Val)) / 16; ++b)
                 cp_async16(dst + b * (16 / sizeof(Val)), inp + i0 + b * (16 / sizeof(Val)));
         }
         cp_async_commit();
-    };
-    auto load_raw = [&](int ts) {
-        const int cl = ts - jr - kl;
-        cp_async_wait<1>();  // all but the group of step ts + 1
-        if (!line_ok || cl < 0 || cl >= Cl) return;
-        const Val* src = &s_pf[wid][ts % NPF][lane][0];
-#pragma unroll
-        for (int e = 0; e < CH; ++e) ra[e] = src[e];
-    };
-    Val pre[CH];
-    auto make_pre = [&](int ts) {
-        const int cl = ts - jr - kl;
-        if (!line_ok || cl < 0 || cl >= Cl) return;
-#pragma unroll
-        for (int e = 0; e < CH; ++e) pre[e] = MODE == SW_BWD ? p0 * ra[e] : ra[e];
     };
     const Val bnd = MODE == SW_GS ? F[0] : Val(0);  // GS: U(0), the inflow boundary value of the line
     issue_raw(T0);
@@ -297,32 +308,42 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
     int abort = 0;
 
     for (int T = T0; T <= T1; ++T) {
-        const int cl = T - jr - kl;
-        const bool act = line_ok && cl >= 0 && cl < Cl;
-        const int c = MODE == SW_BWD ? c_hi - cl : c_lo + cl;
-        const int i0 = CH * c;
-        const bool edge = (c == 0) || (c == C - 1);
-        if (cl == 0) carry = Val(0);  // first chunk of the line in this block: nothing before it
-        const Val cbnd = bnd;
-        // this step's operands, read from the shared-memory slot and scaled
+        const int qb = CH * (T - T0) - dl;  // position of point 0
+        const int aT = chunk_of(T);
+        int ix[CH];
+        bool act[CH], inr[CH];
+#pragma unroll
+        for (int e = 0; e < CH; ++e) {
+            const int q = qb + e;
+            act[e] = line_ok && q >= 0 && q < Q;
+            ix[e] = ibase + idir * q;
+            inr[e] = ix[e] >= 1 && ix[e] <= g.nx - 2;
+        }
+        // this step's operands, read from the shared-memory slots and scaled
         // before the warp waits for its producers.  A register prefetch a
         // step ahead was slower (loads still in flight at the end-of-step
         // release have to complete first); cp.async copies are not ordered
-        // by that release, so they run two steps ahead (box512 FP64 SSOR
-        // sweeps 284 -> 256 ms per step, GS 83 -> 79 ms).
-        load_raw(T);
-        make_pre(T);
+        // by that release, so they run two steps ahead.
+        cp_async_wait<1>();  // all but the group of step T + 1
         Val cur[CH];
 #pragma unroll
-        for (int e = 0; e < CH; ++e) cur[e] = pre[e];
+        for (int e = 0; e < CH; ++e) {
+            cur[e] = Val(0);
+            if (act[e]) {
+                const int q = qb + e;
+                const int slot = (q >> 2) == aT ? T % NPF : (T + NPF - 1) % NPF;
+                const int el = MODE == SW_BWD ? CH - 1 - (q & (CH - 1)) : (q & (CH - 1));
+                const Val r = s_pf[wid][slot][lane][el];
+                cur[e] = MODE == SW_BWD ? p0 * r : r;
+            }
+        }
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
         if (lane == 0) {
-            const int cl0 = T - (32 * cta.jb - jblk0) - kl;
-            if (fj && cl0 >= 0 && cl0 < Cl && !pj_ok && seen_j < T - 1) {
+            if (fj && T - T0 < Cl && !pj_ok && seen_j < T - 1) {
                 seen_j = wait_global(fj, tag, T - 1);
                 if (seen_j < 0) abort = 1;
             }
-            if (kl > 0 && cl0 >= 0 && T - jl_last - kl < Cl) {
+            if (kl > 0) {
                 const int target = min(T - 1, tend_k);
                 if (wid > 0) {
                     if (!wait_cta(&s_prog[wid - 1], target)) abort = 1;
@@ -333,68 +354,58 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             }
         }
         __syncwarp();
-        // ---- predecessors
-        Val pj[CH], pk[CH];
-#pragma unroll
-        for (int e = 0; e < CH; ++e) pj[e] = __shfl_up_sync(0xffffffffu, last[e], 1);
         if (__shfl_sync(0xffffffffu, abort, 0)) {
             if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
             cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
             return;
         }
-        if (act) {
-            if (lane == 0) {
+        // ---- inputs of the plane below (same positions, one step earlier)
+        // and of the row above for lane 0 (chunk-aligned: lane 0 lags by 0)
+        Val pk[CH], pj0[CH];
+        if (wid > 0) {
+            const Val* rs = &s_ring[wid - 1][(T - 1) & (RING - 1)][lane][0];
 #pragma unroll
-                for (int e = 0; e < CH; ++e) pj[e] = pj_ok ? pj_pf[e] : (jin_zero ? Val(0) : __ldcg(jin + i0 + e));
-            }
-            if (wid > 0) {
-                const Val* rs = &s_ring[wid - 1][(T - 1) & (RING - 1)][lane][0];
+            for (int e = 0; e < CH; ++e) pk[e] = act[e] ? rs[e] : Val(0);
+        } else {
 #pragma unroll
-                for (int e = 0; e < CH; ++e) pk[e] = rs[e];
-            } else {
-#pragma unroll
-                for (int e = 0; e < CH; ++e) pk[e] = pk_ok ? pk_pf[e] : (kin_zero ? Val(0) : __ldcg(kin + i0 + e));
-            }
-            if (wrap) {
-#pragma unroll
-                for (int e = 0; e < CH; ++e) cur[e] = fma(p2, __ldcg(Fjp + i0 + e), cur[e]);
-            }
-            Val nv[CH];
-#pragma unroll
-            for (int e = 0; e < CH; ++e) nv[e] = fma(cj, pj[e], fma(ck, pk[e], cur[e]));
-            if (!edge) {
-                if (MODE != SW_BWD) {
-#pragma unroll
-                    for (int e = 0; e < CH; ++e) { carry = fma(ci, carry, nv[e]); nv[e] = carry; }
-                } else {
-#pragma unroll
-                    for (int e = CH - 1; e >= 0; --e) { carry = fma(ci, carry, nv[e]); nv[e] = carry; }
-                }
-            } else {  // first / last chunk: points outside 1..nx-2 are boundary values or zero
-                if (MODE != SW_BWD) {
-                    Val prev = c == 0 ? (MODE == SW_GS ? cbnd : Val(0)) : carry;
-#pragma unroll
-                    for (int e = 0; e < CH; ++e) {
-                        const int i = i0 + e;
-                        if (i >= 1 && i <= g.nx - 2) { prev = fma(ci, prev, nv[e]); nv[e] = prev; }
-                        else { nv[e] = (MODE == SW_GS && i == 0) ? cbnd : Val(0); prev = nv[e]; }
-                    }
-                    carry = prev;
-                } else {
-                    Val prev = c == C - 1 ? Val(0) : carry;
-#pragma unroll
-                    for (int e = CH - 1; e >= 0; --e) {
-                        const int i = i0 + e;
-                        if (i >= 1 && i <= g.nx - 2) { prev = fma(ci, prev, nv[e]); nv[e] = prev; }
-                        else { nv[e] = Val(0); prev = Val(0); }
-                    }
-                    carry = prev;
-                }
-            }
-#pragma unroll
-            for (int e = 0; e < CH; ++e) last[e] = nv[e];
+            for (int e = 0; e < CH; ++e)
+                pk[e] = !act[e] ? Val(0) : (pk_ok ? pk_pf[e] : (kin_zero ? Val(0) : __ldcg(kin + ix[e])));
         }
-        // ---- hand the chunk to the next plane (ring slot T % RING), publish
+#pragma unroll
+        for (int e = 0; e < CH; ++e)
+            pj0[e] = (lane != 0 || !act[e]) ? Val(0) : (pj_ok ? pj_pf[e] : (jin_zero ? Val(0) : __ldcg(jin + ix[e])));
+        if (wrap) {
+#pragma unroll
+            for (int e = 0; e < CH; ++e)
+                if (act[e]) cur[e] = fma(p2, __ldcg(Fjp + ix[e]), cur[e]);
+        }
+#pragma unroll
+        for (int e = 0; e < CH; ++e) cur[e] = fma(ck, pk[e], cur[e]);
+        // ---- the points in sweep order: the (j-1) input of point e is the
+        // neighbour lane's point e - plag (this step) or e - plag + CH (the
+        // step before), by shuffle; lane 0 has it from the row above
+        Val out[CH];
+#pragma unroll
+        for (int e = 0; e < CH; ++e) {
+            const Val src = plag == 1 ? (e == 0 ? last[CH - 1] : out[e > 0 ? e - 1 : 0]) : last[e];
+            Val pj = __shfl_up_sync(0xffffffffu, src, 1);
+            if (lane == 0) pj = pj0[e];
+            const Val nv = fma(cj, pj, cur[e]);
+            out[e] = Val(0);
+            if (act[e]) {
+                if (qb + e == 0) carry = Val(0);  // first position of the block: nothing before it
+                if (inr[e]) {
+                    carry = fma(ci, carry, nv);
+                    out[e] = carry;
+                } else {  // outside 1..nx-2: the GS inflow boundary value, or zero
+                    out[e] = (MODE == SW_GS && ix[e] == 0) ? bnd : Val(0);
+                    carry = out[e];
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < CH; ++e) last[e] = out[e];
+        // ---- hand the points to the next plane (ring slot T % RING), publish
         if (has_down) {
             if (lane == 0 && T - RING + 1 >= T0 + 1)
                 if (!wait_cta(&s_prog[wid + 1], min(T - RING + 1, T1 + 1))) abort = 1;
@@ -406,22 +417,20 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
             }
             Val* ws = &s_ring[wid][T & (RING - 1)][lane][0];
 #pragma unroll
-            for (int e = 0; e < CH; ++e) ws[e] = last[e];
+            for (int e = 0; e < CH; ++e) ws[e] = out[e];
         }
         __syncwarp();
         if (lane == 0) st_release_cta(&s_prog[wid], T);
         // the results go to global memory after the hand-off to the next
         // plane, which reads the ring only, so that release does not wait for
         // these stores; the device-scope progress flag (for the CTAs that
-        // read the rows and planes from global memory) is released after them
-        if (act) {
-            const bool all = !edge || MODE != SW_GS;
+        // read the rows and planes from global memory) is released after them.
+        // GS writes the interior points only (i = 0 holds the boundary value).
 #pragma unroll
-            for (int e = 0; e < CH; ++e) {
-                const int i = i0 + e;
-                const bool in = all || (i >= 1 && i <= g.nx - 2);
-                if (in) outp[i0 + e] = last[e];
-                if (MODE == SW_GS && hout && (edge ? (i >= 1 && i <= g.nx - 2) : true)) hout[i0 + e] = last[e];
+        for (int e = 0; e < CH; ++e) {
+            if (act[e] && (MODE != SW_GS || inr[e])) {
+                outp[ix[e]] = out[e];
+                if (MODE == SW_GS && hout) hout[ix[e]] = out[e];
             }
         }
         if ((T - T0) % PUB == PUB - 1 || T == T1) {
@@ -432,19 +441,22 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         pj_ok = false;
         pk_ok = false;
         if (T < T1) {
-            const int cln = T + 1 - jr - kl;
-            const bool actn = line_ok && cln >= 0 && cln < Cl;
-            const int i0n = CH * (MODE == SW_BWD ? c_hi - cln : c_lo + cln);
-            if (lane == 0 && fj && seen_j >= T && actn) {
+            if (lane == 0 && fj && seen_j >= T) {
 #pragma unroll
-                for (int e = 0; e < CH; ++e) pj_pf[e] = jin_zero ? Val(0) : __ldcg(jin + i0n + e);
+                for (int e = 0; e < CH; ++e) {
+                    const int qn = qb + CH + e;
+                    pj_pf[e] = (jin_zero || !line_ok || qn < 0 || qn >= Q) ? Val(0) : __ldcg(jin + ix[e] + idir * CH);
+                }
                 pj_ok = true;
             }
             if (wid == 0 && fk) {
                 const int pf = __shfl_sync(0xffffffffu, (lane == 0 && seen_k >= min(T, tend_k)) ? 1 : 0, 0);
-                if (pf && actn) {
+                if (pf) {
 #pragma unroll
-                    for (int e = 0; e < CH; ++e) pk_pf[e] = kin_zero ? Val(0) : __ldcg(kin + i0n + e);
+                    for (int e = 0; e < CH; ++e) {
+                        const int qn = qb + CH + e;
+                        pk_pf[e] = (kin_zero || !line_ok || qn < 0 || qn >= Q) ? Val(0) : __ldcg(kin + ix[e] + idir * CH);
+                    }
                 }
                 pk_ok = pf != 0;
             }
@@ -452,7 +464,6 @@ __global__ void __launch_bounds__(KG * 32) k_sweep(SweepArgs<Val> a) {
         issue_raw(T + 2);
     }
     cp_async_wait<0>();
-    (void)tend_j;
 }
 
 // The part of a Gauss-Seidel point update that reads only values the sweep
@@ -708,6 +719,10 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     a.sw = (2 - h->cfg.omega) / h->cfg.omega;
     a.jb_rows = (h->cfg.flags & TBL_FLAG_SSOR_SPAN_BLOCKS) ? 32 : 0;
     a.nib = h->ssor_nib > 0 ? h->ssor_nib : 1;
+    // A row lags the row above by one position.  With 4 span rows or fewer the
+    // Gauss-Seidel wrap row (which reads row 1's new values from global
+    // memory) would share a step with row 1, so those grids lag by a chunk.
+    a.plag = h->g.ny - 2 <= 4 ? CHUNK : 1;
     a.t = -h->cfg.dt / (h->cfg.re);
     return a;
 }
