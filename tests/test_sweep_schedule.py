@@ -1,0 +1,429 @@
+"""The wavefront sweep's schedule (turbulentbl_gb300/csrc/tbl_sweep.cu,
+k_sweep), checked on the CPU.
+
+A model of the kernel's index arithmetic -- positions per lane and step,
+the 32-row block lag, the first and last steps T0/T1 of each warp, the
+two-steps-ahead operand ring, the plane-to-plane ring and the wait targets
+-- runs every warp in global step order.  Data from other warps is read
+from the state as of the end of the previous step, so a read of something
+not yet produced, or already overwritten, gives a different result from the
+sequential lexicographic sweep the reference performs
+(dnstbl2/dnstbl.f90:830-868 Gauss-Seidel, :1022-1042 and :1115-1135 block
+SSOR), which the model also runs.  The model asserts that every wait
+targets a step its producer completes, that every index stays inside its
+buffer and that every operand slot holds the chunk a lane reads from it.
+The same model with a block lag one step short, or with the one-position
+row lag on a 4-row grid (where the kernel keeps a lag of a chunk), must
+disagree with the sequential sweep.
+
+The point arithmetic is a*b + c in both runs (the schedule, not the
+rounding, is under test).
+"""
+import random
+
+import pytest
+
+CH = 4     # points per lane and step (CHUNK)
+KG = 4     # planes (warps) per CTA
+RING = 4   # plane-to-plane slots
+NPF = 4    # operand slots
+
+
+def fma(a, b, c):
+    return a * b + c
+
+
+def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
+    """One sweep of mode 0 (Gauss-Seidel), 1 (forward SSOR) or 2 (backward
+    SSOR) over slabs of K_list planes, J span rows and nx points per line,
+    by the kernel's schedule with row lag plag (and block lag changed by
+    blag_delta) and sequentially.  Returns (points that differ, last step,
+    counts of the waits checked)."""
+    rnd = random.Random(seed)
+    sx = ((nx + 7) + 7) // 8 * 8
+    C = (nx - 2) // CH + 1
+    assert CH * C <= sx
+    CB = (C + nib - 1) // nib
+    nblk = (C + CB - 1) // CB if mode != 0 else 1
+    if mode == 0:
+        nib_ = 1
+    else:
+        nib_ = nib
+    P = len(K_list)
+    ny = J + 2
+    njb = (J + 31) // 32
+    # CTA table
+    ctas = []
+    slabs = []
+    bn = 1
+    for r, K in enumerate(K_list):
+        slabs.append((bn, K))
+        bn += K
+        nkg = (K + KG - 1) // KG
+        base = len(ctas)
+        for kg in range(nkg):
+            for jb in range(njb):
+                ctas.append(dict(slab=r, jb=jb, kg=kg, up_j=base + kg * njb + (jb - 1) if jb > 0 else -1,
+                                 up_k=base + (kg - 1) * njb + jb if kg > 0 else -1))
+    nz = bn + 1
+    ps = sx * ny
+    vol = ps * nz
+    cj, ck, ci, p2 = 0.3, 0.2, 0.4, 0.15
+    if mode == 2:
+        p0 = 1.7
+    inp = [rnd.uniform(-1, 1) for _ in range(vol)]     # PRE (GS) / RH (FWD, BWD)
+    F = [rnd.uniform(-1, 1) for _ in range(vol)]       # GS field (old values); bnd at i = 0
+    halo_in = {}  # (slab) -> plane values for kidx == 0 GS reads (the slab below's top plane snapshot)
+    for r in range(P):
+        halo_in[r] = [rnd.uniform(-1, 1) for _ in range(ps)]
+
+    def idx(i, j, k):
+        assert 0 <= i < sx, i
+        assert 0 <= j < ny
+        assert 0 <= k < nz
+        return i + sx * (j + ny * k)
+
+    # ---------------- sequential reference (lexicographic per slab)
+    Fseq = list(F)
+    RHseq = list(inp)
+    OUTseq = [0.0] * vol
+    for r, (bnr, K) in enumerate(slabs):
+        for bi in range(nblk if mode != 0 else 1):
+            c_lo = bi * CB if mode != 0 else 0
+            c_hi = min(C, c_lo + CB) - 1 if mode != 0 else C - 1
+            Q = CH * (c_hi - c_lo + 1)
+            ibase = CH * c_hi + CH - 1 if mode == 2 else CH * c_lo
+            idir = -1 if mode == 2 else 1
+            for kl in range(K):
+                kidx = K - 1 - kl if mode == 2 else kl
+                k = bnr + kidx
+                for jl in range(J):
+                    jblk0 = (jl // jb_rows) * jb_rows if (mode != 0 and jb_rows > 0) else 0
+                    jr = jl - jblk0
+                    jidx = J - 1 - jl if mode == 2 else jl
+                    j = 1 + jidx
+                    carry = 0.0
+                    bnd = F[idx(0, j, k)] if mode == 0 else 0.0
+                    for q in range(Q):
+                        i = ibase + idir * q
+                        cur = inp[idx(i, j, k)]
+                        if mode == 2:
+                            cur = p0 * cur
+                        inr = 1 <= i <= nx - 2
+                        # wrap (GS, last row reads row 1 new)
+                        if mode == 0 and j == ny - 2:
+                            cur = fma(p2, Fseq[idx(i, 1, k)], cur)
+                        # k input
+                        if mode == 0:
+                            if kidx == 0 and r > 0:
+                                pk = halo_in[r][i + sx * j]
+                            else:
+                                pk = Fseq[idx(i, j, k - 1)]
+                        else:
+                            kin_zero = (kidx == 0) if mode == 1 else (kidx == K - 1)
+                            if kin_zero:
+                                pk = 0.0
+                            else:
+                                pk = (RHseq if mode == 1 else OUTseq)[idx(i, j, k - 1 if mode == 1 else k + 1)]
+                        # j input
+                        if mode == 0:
+                            jm = ny - 2 if j == 1 else j - 1
+                            pj = Fseq[idx(i, jm, k)]
+                        else:
+                            if jr == 0:
+                                pj = 0.0
+                            else:
+                                pj = (RHseq if mode == 1 else OUTseq)[idx(i, j - 1 if mode == 1 else j + 1, k)]
+                        cur = fma(ck, pk, cur)
+                        nv = fma(cj, pj, cur)
+                        if q == 0:
+                            carry = 0.0
+                        if inr:
+                            carry = fma(ci, carry, nv)
+                            o = carry
+                        else:
+                            o = bnd if (mode == 0 and i == 0) else 0.0
+                            carry = o
+                        if mode == 0:
+                            if inr:
+                                Fseq[idx(i, j, k)] = o
+                        elif mode == 1:
+                            RHseq[idx(i, j, k)] = o
+                        else:
+                            OUTseq[idx(i, j, k)] = o
+    # ---------------- the kernel's schedule
+    G = list(F)           # GS field written by the sweep
+    RH = list(inp)        # FWD in place
+    OUT = [0.0] * vol
+    wstep = {}            # global location -> step written
+    warps = []
+    for ci_, cta in enumerate(ctas):
+        for by in range(nib_):
+            for wid in range(KG):
+                warps.append((ci_, by, wid))
+    st = {}
+    ring = {}   # (cta, by, wid, slot) -> (step, [lane][e])
+    maxT = 0
+    info = {}
+    for (cidx, by, wid) in warps:
+        cta = ctas[cidx]
+        bnr, K = slabs[cta['slab']]
+        c_lo = by * CB if mode != 0 else 0
+        c_hi = min(C, c_lo + CB) - 1 if mode != 0 else C - 1
+        Cl = c_hi - c_lo + 1
+        if Cl <= 0:
+            continue
+        kl = KG * cta['kg'] + wid
+        if kl >= K:
+            continue
+        jblk0 = (32 * cta['jb'] // jb_rows) * jb_rows if (mode != 0 and jb_rows > 0) else 0
+        bj = (32 * cta['jb'] - jblk0) >> 5
+        blag = (31 * plag + 2 * CH - 1) // CH + blag_delta
+        lane_last = min(32 * cta['jb'] + 31, J - 1) - 32 * cta['jb']
+        Q = CH * Cl
+        T0 = kl + blag * bj
+        T1 = T0 + (Q - 1 + plag * lane_last) // CH
+        info[(cidx, by, wid)] = dict(T0=T0, T1=T1, kl=kl, K=K, bnr=bnr, c_lo=c_lo, c_hi=c_hi, Cl=Cl, Q=Q,
+                                     jblk0=jblk0, lane_last=lane_last)
+        maxT = max(maxT, T1)
+        st[(cidx, by, wid)] = dict(last=[[0.0] * CH for _ in range(32)], carry=[0.0] * 32,
+                                   slots={}, done=-1)
+    # issue_raw bookkeeping: slots[(lane, slot)] = (chunk, step)
+    def chunk_of(inf, lane, ts):
+        return (CH * (ts - inf['T0']) - plag * lane + CH - 1) >> 2
+
+    def issue(w, ts):
+        inf = info[w]
+        cta = ctas[w[0]]
+        for lane in range(32):
+            jl = 32 * cta['jb'] + lane
+            if not (jl < J):
+                continue
+            ac = chunk_of(inf, lane, ts)
+            if ts <= inf['T1'] and 0 <= ac < inf['Cl']:
+                i0 = CH * (inf['c_hi'] - ac if mode == 2 else inf['c_lo'] + ac)
+                assert i0 % CH == 0 and i0 + CH <= sx
+                st[w]['slots'][(lane, ts % NPF)] = (ac, ts)
+
+    for w in info:
+        issue(w, info[w]['T0'])
+        issue(w, info[w]['T0'] + 1)
+
+    checks = dict(j_wait=0, k_wait=0)
+    for T in range(0, maxT + 1):
+        snapG, snapRH, snapOUT = list(G), list(RH), list(OUT)
+        snap_ring = dict(ring)
+        snap_done = {w: st[w]['done'] for w in st}
+        for w in info:
+            inf = info[w]
+            if not (inf['T0'] <= T <= inf['T1']):
+                continue
+            cidx, by, wid = w
+            cta = ctas[cidx]
+            bnr, K = inf['bnr'], inf['K']
+            kl = inf['kl']
+            T0, T1 = inf['T0'], inf['T1']
+            tend_k = T1 - 1
+            # waits: producers must have completed the target steps (in the snapshot)
+            if cta['up_j'] >= 0 and 32 * cta['jb'] != inf['jblk0'] and T - T0 < inf['Cl']:
+                up = (cta['up_j'], by, wid)
+                tgt = T - 1
+                assert tgt <= info[up]['T1'], ("j target beyond producer's last step", tgt, info[up]['T1'])
+                assert snap_done[up] >= tgt, ("j producer behind", T, snap_done[up], tgt)
+                checks['j_wait'] += 1
+            if kl > 0:
+                tgt = min(T - 1, tend_k)
+                if wid > 0:
+                    up = (cidx, by, wid - 1)
+                else:
+                    up = (cta['up_k'], by, KG - 1)
+                assert info[up]['T1'] == tend_k, ("tend_k", info[up]['T1'], tend_k)
+                assert snap_done[up] >= tgt
+                checks['k_wait'] += 1
+            outs = [[0.0] * CH for _ in range(32)]
+            lanes = []
+            for lane in range(32):
+                jl = 32 * cta['jb'] + lane
+                jr = jl - inf['jblk0']
+                line_ok = jl < J
+                jidx = J - 1 - jl if mode == 2 else jl
+                kidx = K - 1 - kl if mode == 2 else kl
+                j = 1 + max(0, min(jidx, J - 1))
+                k = bnr + kidx
+                jm = ny - 2 if j == 1 else j - 1
+                jp = 1 if j == ny - 2 else j + 1
+                dl = plag * lane
+                qb = CH * (T - T0) - dl
+                aT = chunk_of(inf, lane, T)
+                ibase = CH * inf['c_hi'] + CH - 1 if mode == 2 else CH * inf['c_lo']
+                idir = -1 if mode == 2 else 1
+                act = [line_ok and 0 <= qb + e < inf['Q'] for e in range(CH)]
+                ix = [ibase + idir * (qb + e) for e in range(CH)]
+                inr = [1 <= x <= nx - 2 for x in ix]
+                cur = [0.0] * CH
+                for e in range(CH):
+                    if act[e]:
+                        q = qb + e
+                        assert 0 <= ix[e] < sx
+                        slot = T % NPF if (q >> 2) == aT else (T + NPF - 1) % NPF
+                        assert (q >> 2) in (aT, aT - 1)
+                        ent = st[w]['slots'].get((lane, slot))
+                        assert ent is not None and ent[0] == (q >> 2), ("slot content", ent, q >> 2, T)
+                        assert ent[1] <= T
+                        r_ = inp[idx(ix[e], j, k)]  # operands are inputs, never overwritten before use
+                        if mode == 1:
+                            r_ = snapRH[idx(ix[e], j, k)]
+                            assert r_ == inp[idx(ix[e], j, k)], "FWD operand overwritten before its read"
+                        cur[e] = p0 * r_ if mode == 2 else r_
+                lanes.append(dict(lane=lane, jr=jr, line_ok=line_ok, j=j, k=k, jm=jm, jp=jp, kidx=kidx, qb=qb,
+                                  act=act, ix=ix, inr=inr, cur=cur, jidx=jidx))
+            # pk, pj0, wrap
+            for L in lanes:
+                lane = L['lane']
+                act, ix, j, k = L['act'], L['ix'], L['j'], L['k']
+                pk = [0.0] * CH
+                if wid > 0:
+                    key = (cidx, by, wid - 1, (T - 1) % RING)
+                    ent = snap_ring.get(key)
+                    for e in range(CH):
+                        if act[e]:
+                            assert ent is not None and ent[0] == T - 1, ("ring", ent and ent[0], T - 1)
+                            pk[e] = ent[1][lane][e]
+                else:
+                    for e in range(CH):
+                        if not act[e]:
+                            continue
+                        if mode == 0:
+                            if L['kidx'] == 0 and ctas[cidx]['slab'] > 0:
+                                pk[e] = halo_in[ctas[cidx]['slab']][ix[e] + sx * j]
+                            else:
+                                pk[e] = snapG[idx(ix[e], j, k - 1)]
+                        else:
+                            kin_zero = (L['kidx'] == 0) if mode == 1 else (L['kidx'] == K - 1)
+                            if not kin_zero:
+                                kk = k - 1 if mode == 1 else k + 1
+                                pk[e] = (snapRH if mode == 1 else snapOUT)[idx(ix[e], j, kk)]
+                L['pk'] = pk
+                pj0 = [0.0] * CH
+                if lane == 0:
+                    if mode != 0:
+                        assert L['qb'] % CH == 0 or not any(act)
+                    for e in range(CH):
+                        if not act[e]:
+                            continue
+                        if mode == 0:
+                            pj0[e] = snapG[idx(ix[e], L['jm'], k)]
+                            # row 1 reading the last row: that row must not have been written yet
+                            if L['jidx'] == 0:
+                                assert wstep.get(('G', idx(ix[e], L['jm'], k)), 10 ** 9) > T, "wrap row read after its write"
+                        else:
+                            if L['jr'] != 0:
+                                jj = j - 1 if mode == 1 else j + 1
+                                pj0[e] = (snapRH if mode == 1 else snapOUT)[idx(ix[e], jj, k)]
+                L['pj0'] = pj0
+                if mode == 0 and L['jp'] == 1:
+                    for e in range(CH):
+                        if act[e]:
+                            loc = idx(ix[e], 1, k)
+                            assert wstep.get(('G', loc), -1) < T or not L['inr'][e], "wrap reads row 1 not yet written"
+                            L['cur'][e] = fma(p2, snapG[loc], L['cur'][e])
+                for e in range(CH):
+                    L['cur'][e] = fma(ck, pk[e], L['cur'][e])
+            # the point loop with shuffles (lockstep over lanes)
+            last = st[w]['last']
+            out = [[0.0] * CH for _ in range(32)]
+            for e in range(CH):
+                srcs = []
+                for L in lanes:
+                    lane = L['lane']
+                    if plag == 1:
+                        srcs.append(last[lane][CH - 1] if e == 0 else out[lane][e - 1])
+                    else:
+                        srcs.append(last[lane][e])
+                for L in lanes:
+                    lane = L['lane']
+                    pj = srcs[lane - 1] if lane > 0 else srcs[0]
+                    if lane == 0:
+                        pj = L['pj0'][e]
+                    nv = fma(cj, pj, L['cur'][e])
+                    out[lane][e] = 0.0
+                    if L['act'][e]:
+                        if L['qb'] + e == 0:
+                            st[w]['carry'][lane] = 0.0
+                        if L['inr'][e]:
+                            st[w]['carry'][lane] = fma(ci, st[w]['carry'][lane], nv)
+                            out[lane][e] = st[w]['carry'][lane]
+                        else:
+                            bnd = F[idx(0, L['j'], L['k'])] if mode == 0 else 0.0
+                            out[lane][e] = bnd if (mode == 0 and L['ix'][e] == 0) else 0.0
+                            st[w]['carry'][lane] = out[lane][e]
+            st[w]['last'] = [list(o) for o in out]
+            # ring
+            has_down = wid < KG - 1 and kl + 1 < K
+            if has_down:
+                ring[(cidx, by, wid, T % RING)] = (T, [list(o) for o in out])
+            # stores
+            for L in lanes:
+                for e in range(CH):
+                    if L['act'][e] and (mode != 0 or L['inr'][e]):
+                        loc = idx(L['ix'][e], L['j'], L['k'])
+                        if mode == 0:
+                            G[loc] = out[L['lane']][e]
+                            wstep[('G', loc)] = T
+                        elif mode == 1:
+                            RH[loc] = out[L['lane']][e]
+                        else:
+                            OUT[loc] = out[L['lane']][e]
+            st[w]['done'] = T
+            issue(w, T + 2)
+    # compare
+    ref = Fseq if mode == 0 else (RHseq if mode == 1 else OUTseq)
+    got = G if mode == 0 else (RH if mode == 1 else OUT)
+    bad = sum(1 for a, b in zip(ref, got) if a != b)
+    return bad, maxT, checks
+
+
+def kernel_plag(J):
+    """The row lag the host picks for a grid with J span rows (base_args)."""
+    return CH if J <= 4 else 1
+
+
+def _cases():
+    out = []
+    for mode in (0, 1, 2):
+        for nx in (8, 12, 17, 23):
+            for J in (4, 5, 6, 9, 33, 40, 70):
+                for Ks in ((3,), (5, 4), (9,), (2, 6, 5)):
+                    opts = ((0, 1),) if mode == 0 else ((0, 1), (32, 1), (0, 2), (32, 3))
+                    for jb_rows, nib in opts:
+                        out.append((mode, nx, J, Ks, jb_rows, nib))
+    rnd = random.Random(7)
+    return rnd.sample(out, 160)
+
+
+@pytest.mark.parametrize("mode,nx,J,Ks,jb_rows,nib", _cases())
+def test_schedule_reproduces_the_sequential_sweep(mode, nx, J, Ks, jb_rows, nib):
+    bad, _, checks = run(mode, nx, J, list(Ks), kernel_plag(J), jb_rows, nib)
+    assert bad == 0
+    if J > 32 and not (mode != 0 and jb_rows):
+        assert checks["j_wait"] > 0  # blocks below the first wait on the block above
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_chunk_lag_schedule_also_holds(mode):
+    """plag = CH is the schedule of grids with 4 span rows or fewer; it is
+    valid on every grid."""
+    for J in (5, 33, 40):
+        assert run(mode, 12, J, [5, 4], CH)[0] == 0
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_a_block_lag_one_step_short_breaks_the_order(mode):
+    bad, _, _ = run(mode, 12, 40, [3], 1, blag_delta=-1)
+    assert bad > 0
+
+
+def test_one_position_lag_breaks_the_gs_wrap_on_four_rows():
+    assert run(0, 12, 4, [3], 1)[0] > 0
+    assert run(0, 12, 4, [3], CH)[0] == 0
+    assert run(1, 12, 4, [3], 1)[0] == 0  # SSOR has no wrap row
