@@ -148,13 +148,14 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 //   FWD: x = w'*r + w'*As*x(j-1) + w'*Ab*x(k-1) + w'*Aw*x(i-1),   w' = -w/Ap
 //   BWD: y = w'*s*rhat + w'*As*y(j+1) + w'*At*y(k+1) + w'*Aw*y(i+1)
 // which changes only the rounding of the reference's left-to-right sums.
-// Operands of step T that do not depend on other lines are loaded at the
-// start of the step, before the warp waits for its producers; the (k-1) values
-// of the plane below come through a shared memory ring (RING steps deep, with
-// back-pressure), the (j-1) values of the row above by shuffle or, for lane
-// 0, from global memory.
-// FP32 sweeps keep 6 CTAs per SM (80 registers), FP64 ones 4, so that the Gauss-Seidel
-// sweeps of two velocity components stay co-resident on large grids.
+// Operands of step T that do not depend on other lines arrive in shared
+// memory two steps ahead (cp.async) and are read before the warp waits for
+// its producers; the (k-1) values of the plane below come through a shared
+// memory ring (RING steps deep, with back-pressure), the (j-1) values of the
+// row above by shuffle within the step or, for lane 0, from global memory.
+// FP32 sweeps keep 6 CTAs per SM (80 registers), FP64 ones 4, so that the
+// Gauss-Seidel sweeps of two velocity components stay co-resident on large
+// grids.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(SweepArgs<Val> a) {
     constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
