@@ -18,6 +18,7 @@ def lib():
         _lib.orc_solve_ppe.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int32)]
         _lib.orc_flux_shear.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.orc_thicknesses.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 6
     return _lib
 
 
@@ -53,3 +54,14 @@ class OracleRunner(AbiRunner):
         lib().orc_flux_shear(self._h, ub.ctypes.data_as(C.POINTER(C.c_double)),
                              tau.ctypes.data_as(C.POINTER(C.c_double)))
         return ub, tau
+
+    def thicknesses(self, usum2):
+        """bltkns, deltastar, theta, H, Re_theta (each nx) of the rescaling
+        bookkeeping for the time-mean streamwise velocity usum2 (nx x nz);
+        bltkns starts from the handle's current value."""
+        u = np.asfortranarray(usum2, dtype=np.float64)
+        outs = [np.zeros(self.mesh.nx) for _ in range(5)]
+        dp = C.POINTER(C.c_double)
+        st = lib().orc_thicknesses(self._h, u.ctypes.data_as(dp), *[x.ctypes.data_as(dp) for x in outs])
+        assert st == 0
+        return outs

@@ -914,6 +914,44 @@ void accumulate_stats(Oracle& o) {
 }
 
 // ------------------------------------------- a10: rescaling bookkeeping
+// Boundary-layer thickness: the first x3(k) where the time mean reaches
+// 0.99 Ue (dnstbl2/dnstbl.f90:2150-2158).
+static void bl_thickness(Oracle& o) {
+    const int nx = o.nx, nz = o.nz;
+    const double ue = o.c.ue;
+    for (int i = 1; i <= nx; ++i)
+        for (int k = 1; k <= nz; ++k)
+            if (o.usum2[o.id2(i, k)] >= (0.99 * ue)) { o.bltkns[i - 1] = o.x3[k - 1]; break; }
+}
+
+// Displacement and momentum thickness, shape factor and Re_theta per i
+// (dnstbl2/dnstbl.f90:2232-2256): left sums of (1 - u/Ue) and
+// u/Ue (1 - u/Ue) over the cells [x3(k), x3(k+1)], the displacement sum
+// stopping after the cell that starts at bltkns, the momentum sum after the
+// first cell starting at or above it.  The reference accumulates into
+// arrays that it zeroes only after the first use (:218-221, :2270-2271);
+// these sums start at zero.
+static void integral_thicknesses(Oracle& o) {
+    const int nx = o.nx, nz = o.nz;
+    const double ue = o.c.ue, re = o.c.re;
+    for (int i = 1; i <= nx; ++i) {
+        double ds = 0.0;
+        for (int k = 1; k <= nz - 1; ++k) {
+            ds = ds + ((1.0 - (o.usum2[o.id2(i, k)] / ue)) * (o.x3[k] - o.x3[k - 1]));
+            if (o.x3[k - 1] == o.bltkns[i - 1]) break;
+        }
+        o.deltastar[i - 1] = ds;
+        double th = 0.0;
+        for (int k = 1; k <= nz - 1; ++k) {
+            th = th + ((o.usum2[o.id2(i, k)] / ue) * (1.0 - (o.usum2[o.id2(i, k)] / ue)) * (o.x3[k] - o.x3[k - 1]));
+            if (o.x3[k - 1] >= o.bltkns[i - 1]) break;
+        }
+        o.theta[i - 1] = th;
+        o.Ht[i - 1] = ds / th;
+        o.Reth[i - 1] = th * re * ue;
+    }
+}
+
 // dnstbl2/dnstbl.f90:2084-2365
 void rescale(Oracle& o) {
     const int nx = o.nx, ny = o.ny, nz = o.nz, irec = o.c.irec;
@@ -928,9 +966,7 @@ void rescale(Oracle& o) {
     double utau1 = std::sqrt(((o.usum2[o.id2(1, 2)] - o.usum2[o.id2(1, 1)]) / (o.x3[1] - o.x3[0])) / re);
     double utau2 = std::sqrt(((o.usum2[o.id2(irec, 2)] - o.usum2[o.id2(irec, 1)]) / (o.x3[1] - o.x3[0])) / re);
     o.lamda = (utau1) / (utau2);
-    for (int i = 1; i <= nx; ++i)
-        for (int k = 1; k <= nz; ++k)
-            if (o.usum2[o.id2(i, k)] >= (0.99 * ue)) { o.bltkns[i - 1] = o.x3[k - 1]; break; }
+    bl_thickness(o);
     o.lamda03 = o.bltkns[irec - 1] / o.bltkns[0];
     for (int i = 1; i <= nx; ++i)
         for (int k = 1; k <= nz; ++k) {
@@ -953,22 +989,7 @@ void rescale(Oracle& o) {
     for (int k = o.ksep + 1; k <= nz - 1; ++k)
         if (counter <= nz - 1)
             if (o.x3[k - 1] >= zrecy[counter]) { o.newk[counter - 1] = k; counter = counter + 1; }
-    for (int i = 1; i <= nx; ++i) {
-        double ds = 0.0;
-        for (int k = 1; k <= nz - 1; ++k) {
-            ds = ds + ((1.0 - (o.usum2[o.id2(i, k)] / ue)) * (o.x3[k] - o.x3[k - 1]));
-            if (o.x3[k - 1] == o.bltkns[i - 1]) break;
-        }
-        o.deltastar[i - 1] = ds;
-        double th = 0.0;
-        for (int k = 1; k <= nz - 1; ++k) {
-            th = th + ((o.usum2[o.id2(i, k)] / ue) * (1.0 - (o.usum2[o.id2(i, k)] / ue)) * (o.x3[k] - o.x3[k - 1]));
-            if (o.x3[k - 1] >= o.bltkns[i - 1]) break;
-        }
-        o.theta[i - 1] = th;
-        o.Ht[i - 1] = ds / th;
-        o.Reth[i - 1] = th * re * ue;
-    }
+    integral_thicknesses(o);
     // refresh Ufluc(irec,:,k,:) on every rank's own slab (:2341-2349);
     // dnssetbl refreshes rank 0's slab only (dnssetbl.f90:1016, :1033-1041)
     const int kr0 = is_sete(o) ? o.bn[0] : 2, kr1 = is_sete(o) ? o.en[0] : nz - 1;
@@ -1244,6 +1265,25 @@ int orc_apply_ssor(orc_handle* h, const double* x, double* y) {
     std::vector<double> X(x, x + o.N);
     ssor(o, X);
     std::memcpy(y, o.rhat.data(), o.N * 8);
+    return TBL_OK;
+}
+
+// The thicknesses of the rescaling bookkeeping from a given time-mean
+// streamwise velocity usum2 (nx x nz, column-major): bltkns, deltastar,
+// theta, H and Re_theta (each nx), by the same code as the step.
+int orc_thicknesses(orc_handle* h, const double* usum2, double* bltkns, double* deltastar, double* theta,
+                    double* ht, double* reth) {
+    if (!h || !usum2) return TBL_ERR_BAD_ARG;
+    Oracle& o = h->o;
+    std::memcpy(o.usum2.data(), usum2, (size_t)o.nx * o.nz * 8);
+    bl_thickness(o);
+    integral_thicknesses(o);
+    const size_t b = (size_t)o.nx * 8;
+    if (bltkns) std::memcpy(bltkns, o.bltkns.data(), b);
+    if (deltastar) std::memcpy(deltastar, o.deltastar.data(), b);
+    if (theta) std::memcpy(theta, o.theta.data(), b);
+    if (ht) std::memcpy(ht, o.Ht.data(), b);
+    if (reth) std::memcpy(reth, o.Reth.data(), b);
     return TBL_OK;
 }
 

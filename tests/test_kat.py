@@ -5,7 +5,8 @@ to the mathematics it discretises and to its own ordering semantics:
 manufactured solutions for the stretched-grid Laplacian, the GMRES/SSOR
 solve against a direct sparse solve, exactness of the convection stencils on
 polynomials, the lexicographic Gauss-Seidel against a hyperplane-ordered one
-(the ordering the GPU wavefront uses), and the recycling index map.
+(the ordering the GPU wavefront uses), the recycling index map, and the
+boundary-layer, displacement and momentum thicknesses of the rescaling.
 """
 import numpy as np
 import pytest
@@ -185,3 +186,56 @@ def test_mass_flux_and_wall_shear_known_answers():
     expect = (mesh.ny - 2) * (a + b) / rp.re
     assert np.allclose(tau[1:-1], expect, rtol=1e-10)
     assert tau[0] == 0.0 and tau[-1] == 0.0
+
+
+def _uniform_x3_runner(nx=8, nz=40, h=0.05, ue=1.0, re=1000.0):
+    mesh = make_mesh(nx, 6, nz, 3.0, 2.0, 2.0, 2.0)
+    mesh.x3 = np.ascontiguousarray(h * np.arange(nz, dtype=np.float64))
+    rp = RunParams(dt=1e-3, re=re, ue=ue, nproc=2, irec=max(2, nx // 2))
+    return mesh, rp, OracleRunner(mesh, rp)
+
+
+@pytest.mark.parametrize("ue", [1.0, 19.798])
+def test_integral_thicknesses_of_linear_profiles(ue):
+    """u = Ue min(x3/delta, 1) on a uniform x3 (spacing h, delta = m h,
+    m < 100) has bltkns = delta (the first point at or above 0.99 Ue), and the
+    reference's left sums (dnstbl2/dnstbl.f90:2234-2256) give
+    delta* = h (m+1)/2, theta = h (m+1)(m-1)/(6m), H = 3m/(m-1) and
+    Re_theta = theta Re Ue."""
+    h, re = 0.05, 1000.0
+    mesh, rp, o = _uniform_x3_runner(h=h, ue=ue, re=re)
+    ms = np.array([3, 5, 8, 12, 17, 23, 30, 38])
+    u = ue * np.minimum(mesh.x3[None, :] / (ms[:, None] * h), 1.0)
+    bl, ds, th, ht, rt = o.thicknesses(u)
+    assert np.array_equal(bl, mesh.x3[ms])
+    assert np.allclose(ds, h * (ms + 1) / 2, rtol=1e-13, atol=0)
+    assert np.allclose(th, h * (ms + 1) * (ms - 1) / (6 * ms), rtol=1e-13, atol=0)
+    assert np.allclose(ht, 3 * ms / (ms - 1), rtol=1e-13, atol=0)
+    assert np.allclose(rt, th * re * ue, rtol=1e-15, atol=0)
+
+
+def test_integral_thicknesses_keep_the_previous_edge():
+    """When no point reaches 0.99 Ue, bltkns keeps its previous value
+    (dnstbl2/dnstbl.f90:2150-2158).  The displacement sum stops after the
+    cell that starts exactly at bltkns (:2237), the momentum sum after the
+    first cell starting at or above it (:2245): with an edge between two grid
+    points (a value from the restart state) the displacement sum runs over
+    every cell and the momentum sum stops at the next point above the edge."""
+    wl = small_workload(nx=10, nz_span=6, ny_wall=24)
+    mesh, rp, st = make_state(wl, nproc=2)
+    o = OracleRunner(mesh, rp)
+    x3 = mesh.x3
+    edge = 0.5 * (x3[10] + x3[11])
+    o.upload(dict(st, bltkns=np.full(mesh.nx, edge)))
+    r = 0.5 * x3 / x3[-1]  # u / Ue, never reaches 0.99
+    bl, ds, th, _, _ = o.thicknesses(np.tile(rp.ue * r, (mesh.nx, 1)))
+    assert np.all(bl == edge)
+    dz = np.diff(x3)
+    assert np.allclose(ds, np.sum((1 - r[:-1]) * dz), rtol=1e-13, atol=0)
+    assert np.allclose(th, np.sum((r * (1 - r))[:12] * dz[:12]), rtol=1e-13, atol=0)
+    # a new edge on a grid point ends both sums at that point's cell
+    bl, ds, th, _, _ = o.thicknesses(np.tile(rp.ue * np.minimum(x3 / x3[7], 1.0), (mesh.nx, 1)))
+    r = np.minimum(x3 / x3[7], 1.0)
+    assert np.all(bl == x3[7])
+    assert np.allclose(ds, np.sum((1 - r[:8]) * dz[:8]), rtol=1e-13, atol=0)
+    assert np.allclose(th, np.sum((r * (1 - r))[:8] * dz[:8]), rtol=1e-13, atol=0)
