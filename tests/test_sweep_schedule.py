@@ -427,3 +427,24 @@ def test_one_position_lag_breaks_the_gs_wrap_on_four_rows():
     assert run(0, 12, 4, [3], 1)[0] > 0
     assert run(0, 12, 4, [3], CH)[0] == 0
     assert run(1, 12, 4, [3], 1)[0] == 0  # SSOR has no wrap row
+
+
+def test_model_mirrors_the_kernel_source():
+    """The formulas this model restates, as they appear in the kernel and its
+    host glue (a change to either side must be made to both)."""
+    from pathlib import Path
+    src = (Path(__file__).resolve().parents[1] / "turbulentbl_gb300" / "csrc" / "tbl_sweep.cu").read_text()
+    for line in (
+        "const int blag = (31 * plag + 2 * CH - 1) / CH;",
+        "const int T0 = kl + blag * bj;",
+        "const int T1 = T0 + (Q - 1 + plag * lane_last) / CH;",
+        "const int dl = plag * lane;",
+        "auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };",
+        "const int qb = CH * (T - T0) - dl;",
+        "const int slot = (q >> 2) == aT ? T % NPF : (T + NPF - 1) % NPF;",
+        "const int el = MODE == SW_BWD ? CH - 1 - (q & (CH - 1)) : (q & (CH - 1));",
+        "a.plag = h->g.ny - 2 <= 4 ? CHUNK : 1;",
+        "constexpr int RING = 4;",
+        "constexpr int NPF = 4;",
+    ):
+        assert line in src, line
