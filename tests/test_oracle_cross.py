@@ -16,8 +16,11 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("nx,nzs,nyw,P,steps", [(16, 8, 14, 2, 7), (14, 6, 17, 3, 6), (12, 10, 11, 1, 6)])
+@pytest.mark.parametrize("nx,nzs,nyw,P,steps", [(16, 8, 14, 2, 7), (14, 6, 17, 3, 6), (12, 10, 11, 1, 6),
+                                                 (20, 4, 16, 2, 3), (22, 5, 16, 2, 3)])
 def test_cpp_equals_numpy(nx, nzs, nyw, P, steps):
+    """Including the smallest span (4 rows, the periodic wrap of the span
+    stencils on the fewest points) and 5 rows."""
     wl = small_workload(nx=nx, nz_span=nzs, ny_wall=nyw, kmax=10)
     mesh, rp, st = make_state(wl, nproc=P)
     o = OracleRunner(mesh, rp)
