@@ -39,14 +39,33 @@ __global__ void __launch_bounds__(RED_THREADS, 8) k_dot(long long n2, const doub
     grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, op);
 }
 
+// L2 eviction-priority policy for data that should stay in L2 across
+// kernels (evict-last), and 16-byte loads and stores under it.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ double2 ld_keep(const double2* a, unsigned long long pol) {
+    double2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_keep(double2* a, double2 v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(a), "d"(v.x), "d"(v.y), "l"(pol)
+                 : "memory");
+}
+
 // One modified Gram-Schmidt pass (:1140-1150):
 //   w -= (*hk) * vk          (skipped when vk == nullptr)
 //   *out = sum(vn * w)       (vn == nullptr: sum(w*w), op 1 takes the sqrt)
-// Two elements per thread per iteration with evict-first loads and stores
-// (the three vectors, 207 MB at 512x130x128, are far larger than L2), on a
-// grid of MGS_BLOCKS_PER_SM blocks per SM: 1.01 of the measured copy
-// bandwidth in a stand-alone copy, against 0.78 with one element, default
-// caching and 8 blocks per SM.
+// Two elements per thread per iteration on a grid of MGS_BLOCKS_PER_SM
+// blocks per SM.  The basis vectors stream through with evict-first loads;
+// w, read and written by every pass of an Arnoldi step (69 MB at
+// 512x130x128, inside the 129 MB L2), is loaded and stored evict-last so
+// that it stays in L2 from pass to pass.  With everything evict-first a
+// pass ran at 1.01 of the measured copy bandwidth in a stand-alone copy
+// (0.78 with one element, default caching and 8 blocks per SM).
 constexpr int MGS_BLOCKS_PER_SM = 4;
 __global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __restrict__ w,
                                                   const double2* __restrict__ vk, const double* __restrict__ hk,
@@ -54,19 +73,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __re
                                                   int op) {
     __shared__ double s_red[RED_THREADS / 32];
     const double hv = vk ? *hk : 0.0;
+    const unsigned long long keep = l2_keep_policy();
     double acc = 0.0;
     const long long st = (long long)gridDim.x * blockDim.x;
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     for (; q + st < n2; q += 2 * st) {
-        double2 x0 = __ldcs(w + q), x1 = __ldcs(w + q + st);
+        double2 x0 = ld_keep(w + q, keep), x1 = ld_keep(w + q + st, keep);
         if (vk) {
             const double2 v0 = __ldcs(vk + q), v1 = __ldcs(vk + q + st);
             x0.x = x0.x - hv * v0.x;
             x0.y = x0.y - hv * v0.y;
             x1.x = x1.x - hv * v1.x;
             x1.y = x1.y - hv * v1.y;
-            __stcs(w + q, x0);
-            __stcs(w + q + st, x1);
+            st_keep(w + q, x0, keep);
+            st_keep(w + q + st, x1, keep);
         }
         const double2 y0 = vn ? __ldcs(vn + q) : x0, y1 = vn ? __ldcs(vn + q + st) : x1;
         acc += y0.x * x0.x;
@@ -75,12 +95,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __re
         acc += y1.y * x1.y;
     }
     if (q < n2) {
-        double2 x = __ldcs(w + q);
+        double2 x = ld_keep(w + q, keep);
         if (vk) {
             const double2 v = __ldcs(vk + q);
             x.x = x.x - hv * v.x;
             x.y = x.y - hv * v.y;
-            __stcs(w + q, x);
+            st_keep(w + q, x, keep);
         }
         const double2 y = vn ? __ldcs(vn + q) : x;
         acc += y.x * x.x;
