@@ -250,16 +250,17 @@ int tbl_profile_read(tbl_handle* h, double* ms, double* bytes, int64_t* launches
  * cannot allocate device memory (a host code whose own pool allocator owns
  * every byte of the GPU, or a time loop in which an allocation could
  * synchronise the device).  It computes the reference's divergence printout
- * |sum div U| / ((nx-2)(ny-2)(nz-2)) (the value tbl_step reports as div_diag)
- * for fields the caller already holds on the current device, and allocates
+ * |sum div U| / ((nx-2)(ny-2)(nz-2)) (the value tbl_step reports as div_diag;
+ * its square root for cfg->variant == TBL_VARIANT_ORIGINAL) for fields the caller already holds on the current device, and allocates
  * nothing: its only scratch is a fixed array of TBL_NOALLOC_BLOCKS doubles in
  * the library image, held by every GPU that loads the library until exit.
- *   cfg     grid sizes and dx, dy, dxi (other fields unused)
+ *   cfg     grid sizes, dx, dy, dxi and variant (other fields unused)
  *   jacinv  device, nz doubles: 1/Jac(k)
  *   u,v,w   device, nx*ny*nz doubles each, the reference layout (i fastest)
  *   out     device, one double receiving the result
- * Runs asynchronously on the legacy default stream.  The first call on a
- * device looks up the scratch address (make it before any stream capture).
+ * Runs asynchronously on the legacy default stream.  Every call looks up the
+ * scratch address on the current device; the first call on a device also
+ * loads the library's kernels there (make it before any stream capture).
  * Calls share the scratch: calls that overlap on the GPU race.  Grids with
  * more than TBL_NOALLOC_MAX_POINTS interior points are rejected with
  * TBL_ERR_TOO_LARGE. */
@@ -400,6 +401,15 @@ int tbl_counters_read(const char* dir, int32_t* nz, int32_t* cnt, int32_t* nproc
  * per k, FORMAT(4(1X,F15.7),I5.3) (dnssetbl/dnssetbl.f90:1203-1208, 136-140). */
 int tbl_statdata_write(const char* path, int32_t nx, int32_t nz, int32_t irec, const tbl_state* st);
 int tbl_statdata_read(const char* path, int32_t nx, int32_t nz, int32_t irec, tbl_state* st);
+/* The inflow mean profile file U_innerdns.dat (dnssetbl: Input/initProf.dat):
+ * 37 records FORMAT(24X,E18.8), plane 37's value repeated above it
+ * (dnstbl2/dnstbl.f90:322-345; originalTBL/fnldnstbl.f90:411-423;
+ * dnssetbl/dnssetbl.f90:105-114).  The read fills ume1[0..nz-1] (records
+ * beyond nz are read and dropped); the write puts k and x3(k) in the 24
+ * skipped columns and needs nz >= 37. */
+#define TBL_INFLOW_RECORDS 37
+int tbl_inflow_profile_read(const char* path, int32_t nz, double* ume1);
+int tbl_inflow_profile_write(const char* path, int32_t nz, const double* x3, const double* ume1);
 
 #ifdef __cplusplus
 }

@@ -226,3 +226,55 @@ def write_statdata(path, st, irec):
             nk = str(int(st["newk"][k])).zfill(3).rjust(5)
             f.write(f" {st['usum2'][ir, k]:15.7f} {st['vsum2'][ir, k]:15.7f} {st['wsum2'][ir, k]:15.7f}"
                     f" {st['wt'][0, k]:15.7f}{nk}\n")
+
+
+INFLOW_RECORDS = 37
+
+
+def fortran_read_e(field, d):
+    """One Fortran Ew.d input field as a formatted READ with BLANK='NULL'
+    reads it: blanks ignored (all blank = 0), exponent letter E, D or Q or a
+    bare sign, d implied decimals when the mantissa has no point."""
+    t = "".join(ch for ch in field if not ch.isspace())
+    if not t:
+        return 0.0
+    p, mant = 0, ""
+    if t[0] in "+-":
+        mant, p = t[0], 1
+    point = digits = False
+    while p < len(t) and (t[p].isdigit() or (t[p] == "." and not point)):
+        point |= t[p] == "."
+        digits |= t[p].isdigit()
+        mant += t[p]
+        p += 1
+    if not digits:
+        raise ValueError(field)
+    ex = 0
+    if p < len(t):
+        rest = t[p:]
+        if rest[0].upper() in "EDQ":
+            rest = rest[1:]
+        if not rest or not (rest.lstrip("+-").isdigit() and rest[0] in "+-0123456789") or rest.count("+") + rest.count("-") > 1:
+            raise ValueError(field)
+        ex = int(rest)
+    if not point:
+        ex -= d
+    return float(f"{mant}E{ex}")
+
+
+def inflow_profile_text(x3, ume1):
+    """U_innerdns.dat as the library writes it: (1X,I4,1X,E18.8,1X,E18.8)
+    records k, x3(k), Ume1(k) for k = 1..37."""
+    return "".join(f" {k + 1:4d}" + " " + fortran_e(float(x3[k]), 18, 8) + fortran_e(float(ume1[k]), 18, 8) + "\n"
+                   for k in range(INFLOW_RECORDS))
+
+
+def read_inflow_profile(text, nz):
+    """FORMAT(24X,E18.8) on 37 records, record 37 repeated above plane 37
+    (dnstbl2/dnstbl.f90:322-345)."""
+    recs = text.split("\n")
+    if len(recs) < INFLOW_RECORDS or (len(recs) == INFLOW_RECORDS and recs[-1] == ""):
+        raise ValueError("fewer than 37 records")
+    vals = [fortran_read_e(r.ljust(42)[24:42], 8) for r in recs[:INFLOW_RECORDS]]
+    out = np.array([vals[min(k, INFLOW_RECORDS - 1)] for k in range(nz)])
+    return out

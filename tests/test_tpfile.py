@@ -176,3 +176,43 @@ def test_restart_through_files_continues_the_run(tmp_path, P):
         err = np.linalg.norm(runs[1][f] - runs[0][f]) / np.linalg.norm(runs[0][f])
         assert err <= 1e-9, (f, err)
     assert runs[1]["nstep"] == runs[0]["nstep"] == d["nstep"] + 3
+
+
+def test_inflow_profile_round_trip(tmp_path):
+    """U_innerdns.dat written from a profile and read back: 8 significant
+    digits (E18.8), byte-identical to the Python restatement, record 37
+    repeated above plane 37."""
+    wl = small_workload(nx=10, nz_span=6, ny_wall=48)
+    mesh, rp, st = make_state(wl, nproc=2)
+    p = tmp_path / "U_innerdns.dat"
+    tpfile.write_inflow_profile(p, mesh.x3, st["ume1"])
+    assert p.read_text() == ref.inflow_profile_text(mesh.x3, st["ume1"])
+    back = tpfile.read_inflow_profile(p, mesh.nz)
+    assert np.array_equal(back, ref.read_inflow_profile(p.read_text(), mesh.nz))
+    np.testing.assert_allclose(back[:37], st["ume1"][:37], rtol=5e-8, atol=0)
+    assert np.all(back[37:] == back[36])
+
+
+def test_inflow_profile_fortran_input_forms(tmp_path):
+    """Fields as a Fortran READ(…,'(24X,E18.8)') takes them: exponent letters
+    E and D, a bare-sign exponent, no decimal point (8 implied decimals),
+    embedded blanks ignored, an empty field read as zero; a short record is
+    padded with blanks."""
+    fields = ["0.12345678E+01", "1.5D-02", "  .5E0", "12345678", "-0.25+01", "", "1 .5", "3.0E 1"]
+    want = [1.2345678, 0.015, 0.5, 0.12345678, -2.5, 0.0, 1.5, 30.0]
+    recs = [("x" * 24 + f.rjust(18)) for f in fields] + ["x" * 24 + "0.9E0"] * (37 - len(fields))
+    text = "\n".join(recs) + "\n"
+    p = tmp_path / "U_innerdns.dat"
+    p.write_text(text)
+    got = tpfile.read_inflow_profile(p, 40)
+    np.testing.assert_allclose(got[:len(want)], want, rtol=1e-15, atol=0)
+    assert np.all(got[len(want):] == 0.9)
+    assert np.array_equal(got, ref.read_inflow_profile(text, 40))
+    short = tmp_path / "short.dat"
+    short.write_text("\n".join(recs[:36]) + "\n")
+    with pytest.raises(Exception):
+        tpfile.read_inflow_profile(short, 40)
+    bad = tmp_path / "bad.dat"
+    bad.write_text("\n".join(["x" * 24 + "abc"] + recs[1:]) + "\n")
+    with pytest.raises(Exception):
+        tpfile.read_inflow_profile(bad, 40)

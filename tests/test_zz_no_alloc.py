@@ -27,11 +27,14 @@ def _bind(lib):
     return f
 
 
-def test_noalloc_matches_step_diagnostic_twice():
+@pytest.mark.parametrize("variant", [abi.TBL_VARIANT_DNSTBL2, abi.TBL_VARIANT_ORIGINAL])
+def test_noalloc_matches_step_diagnostic_twice(variant):
+    """The default program prints |sum div U|/N, originalTBL its square root."""
     import torch
     from turbulentbl_gb300.lib import TblGpu, load
     wl = small_workload(nx=40, nz_span=34, ny_wall=33)
     mesh, rp, st = make_state(wl, nproc=4)
+    rp.variant = variant
     g = TblGpu(mesh, rp)
     g.upload(st)
     f = _bind(load())

@@ -12,14 +12,15 @@
 // doubles (32 KB) until the process exits.  The call allocates nothing and
 // calls no allocating library routine.
 //
-// Set-up: the first call on a device (the current device at call time) looks
-// up the device address of the scratch array with cudaGetSymbolAddress and
-// clears the arrival counter; later calls on that device reuse the address.
-// Do that first call before any stream capture.  All calls share the scratch
-// array and it keeps the last call's partial sums: the counter is returned to
-// zero by every completed call, so a call needs no clearing, but calls that
-// overlap on the GPU (different streams, or different host threads) race on
-// the scratch and give wrong results.
+// Set-up: every call looks up the device address of the scratch array and of
+// its arrival counter with cudaGetSymbolAddress, on the device that is current
+// at call time, and checks the return code.  The lookup allocates nothing; on
+// the first call on a device it also loads the library's kernels there, so
+// make that first call before any stream capture.  The counter is zero when
+// the library is loaded and every completed call returns it to zero, so no
+// call needs to clear it.  All calls share the scratch array and it keeps the
+// last call's partial sums; calls that overlap on the GPU (different streams,
+// or different host threads) race on the scratch and give wrong results.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -29,13 +30,9 @@ namespace {
 
 constexpr int NA_THREADS = 256;
 constexpr int NA_BLOCKS = TBL_NOALLOC_BLOCKS;
-constexpr int NA_MAX_DEVICES = 64;
 
 static __device__ __align__(256) double g_na_partial[NA_BLOCKS];
 static __device__ __align__(256) unsigned int g_na_count;
-
-double* g_partial_addr[NA_MAX_DEVICES] = {nullptr};
-unsigned int* g_count_addr[NA_MAX_DEVICES] = {nullptr};
 
 __device__ __forceinline__ double na_warp_sum(double v) {
 #pragma unroll
@@ -56,14 +53,15 @@ __device__ __forceinline__ double na_block_sum(double v, double* smem) {
 
 // The 4th-order divergence sum of dnstbl2/dnstbl.f90:1526-1577 over the
 // interior, fields in the reference layout (i fastest, no padding), divided by
-// (nx-2)(ny-2)(nz-2) in absolute value.  Partial sums go to the scratch
-// array; the last block to arrive sums them in block order.
+// (nx-2)(ny-2)(nz-2) in absolute value; originalTBL prints the square root of
+// that (originalTBL/fnldnstbl.f90:1586), selected by take_sqrt.  Partial sums
+// go to the scratch array; the last block to arrive sums them in block order.
 __global__ void __launch_bounds__(NA_THREADS) k_div_diag_static(int nx, int ny, int nz, double invdx, double invdy,
                                                                double invdxi, const double* __restrict__ U1,
                                                                const double* __restrict__ U2,
                                                                const double* __restrict__ U3,
                                                                const double* __restrict__ jacinv, double* partial,
-                                                               unsigned int* count, double* out) {
+                                                               unsigned int* count, int take_sqrt, double* out) {
     __shared__ double s_red[NA_THREADS / 32];
     __shared__ bool s_last;
     const int ni = nx - 2, J = ny - 2, nk = nz - 2;
@@ -105,21 +103,20 @@ __global__ void __launch_bounds__(NA_THREADS) k_div_diag_static(int nx, int ny, 
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) tot += __ldcg(&partial[b]);
     tot = na_block_sum(tot, s_red);
     if (threadIdx.x == 0) {
-        *out = fabs(tot) / ((double)(ny - 2) * (nx - 2) * (nz - 2));
+        const double d = fabs(tot) / ((double)(ny - 2) * (nx - 2) * (nz - 2));
+        *out = take_sqrt ? sqrt(d) : d;
         *count = 0u;  // ready for the next call
     }
 }
 
-int setup_device(int dev) {
-    if (g_partial_addr[dev] && g_count_addr[dev]) return TBL_OK;
+// Device addresses of the scratch array and its counter on the current device.
+int scratch_addresses(double** partial, unsigned int** count) {
     void* p = nullptr;
     void* c = nullptr;
     if (cudaGetSymbolAddress(&p, g_na_partial) != cudaSuccess) return TBL_ERR_CUDA;
     if (cudaGetSymbolAddress(&c, g_na_count) != cudaSuccess) return TBL_ERR_CUDA;
-    if (cudaMemset(c, 0, sizeof(unsigned int)) != cudaSuccess) return TBL_ERR_CUDA;
-    if (cudaDeviceSynchronize() != cudaSuccess) return TBL_ERR_CUDA;
-    g_partial_addr[dev] = static_cast<double*>(p);
-    g_count_addr[dev] = static_cast<unsigned int*>(c);
+    *partial = static_cast<double*>(p);
+    *count = static_cast<unsigned int*>(c);
     return TBL_OK;
 }
 
@@ -134,15 +131,16 @@ extern "C" int tbl_div_diag_noalloc(const tbl_config* cfg, const double* jacinv,
     if (n > TBL_NOALLOC_MAX_POINTS) return TBL_ERR_TOO_LARGE;  // beyond what the fixed scratch is sized for
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return TBL_ERR_NO_DEVICE;
-    if (dev < 0 || dev >= NA_MAX_DEVICES) return TBL_ERR_BAD_ARG;
-    int s = setup_device(dev);
+    double* partial = nullptr;
+    unsigned int* count = nullptr;
+    int s = scratch_addresses(&partial, &count);
     if (s != TBL_OK) return s;
     long long blocks = (n + (long long)NA_THREADS * 16 - 1) / ((long long)NA_THREADS * 16);
     if (blocks > NA_BLOCKS) blocks = NA_BLOCKS;
     if (blocks < 1) blocks = 1;
     k_div_diag_static<<<(unsigned)blocks, NA_THREADS>>>(cfg->nx, cfg->ny, cfg->nz, 1.0 / cfg->dx, 1.0 / cfg->dy,
-                                                        1.0 / cfg->dxi, u, v, w, jacinv, g_partial_addr[dev],
-                                                        g_count_addr[dev], out);
+                                                        1.0 / cfg->dxi, u, v, w, jacinv, partial, count,
+                                                        cfg->variant == TBL_VARIANT_ORIGINAL ? 1 : 0, out);
     if (cudaGetLastError() != cudaSuccess) return TBL_ERR_CUDA;
     return TBL_OK;
 }

@@ -31,34 +31,37 @@ namespace {
 int ncols(int format) { return format == TBL_TP_DNSTBL2 ? 15 : (format == TBL_TP_ORIGINAL ? 8 : 7); }
 bool valid_format(int f) { return f == TBL_TP_DNSTBL2 || f == TBL_TP_ORIGINAL || f == TBL_TP_DNSSETBL; }
 
-// Fortran Ew.d output (w = 22, d = 15): [-]0.<d digits>E+xx, right-justified.
+// Fortran Ew.d output: [-]0.<d digits>E+xx, right-justified in w columns,
+// after one blank (the 1X before every field of the reference's formats).
 // The d significant digits come from the correctly rounded %.*E conversion;
 // the exponent is one more than C's (mantissa 0.d... instead of d.d...).  An
 // exponent beyond two digits drops the E, as Ew.d does.
-void put_e(std::string& out, double v) {
-    char buf[64], body[40];
+void put_e_wd(std::string& out, double v, int w, int d) {
+    char buf[64], body[64];
     if (v == 0.0) {
-        snprintf(body, sizeof body, "0.000000000000000E+00");
+        snprintf(body, sizeof body, "0.%0*dE+00", d, 0);
     } else if (!std::isfinite(v)) {
         snprintf(body, sizeof body, "%s", std::isnan(v) ? "NaN" : (v > 0 ? "Infinity" : "-Infinity"));
     } else {
-        snprintf(buf, sizeof buf, "%.14E", std::fabs(v));  // d.dddddddddddddd E+xx
+        snprintf(buf, sizeof buf, "%.*E", d - 1, std::fabs(v));  // d.ddd E+xx
         const char* e = strchr(buf, 'E');
         const int ex = atoi(e + 1) + 1;
-        char digits[20];
+        char digits[40];
         digits[0] = buf[0];
-        memcpy(digits + 1, buf + 2, 14);
-        digits[15] = 0;
+        memcpy(digits + 1, buf + 2, (size_t)(d - 1));
+        digits[d] = 0;
         const char* sg = v < 0 ? "-" : "";
         if (ex > 99 || ex < -99)
             snprintf(body, sizeof body, "%s0.%s%c%03d", sg, digits, ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
         else
             snprintf(body, sizeof body, "%s0.%sE%c%02d", sg, digits, ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
     }
-    char field[64];
-    snprintf(field, sizeof field, " %22s", body);
+    char field[80];
+    snprintf(field, sizeof field, " %*s", w, body);
     out += field;
 }
+
+void put_e(std::string& out, double v) { put_e_wd(out, v, 22, 15); }
 
 void put_f(std::string& out, double v, int w, int d) {
     char buf[64];
@@ -202,6 +205,52 @@ bool parse_numbers(const std::string& s, size_t pos, size_t count, std::vector<d
         p = q;
     }
     return true;
+}
+
+// One Fortran Ew.d input field (list of characters already cut to the field
+// width), read as a formatted READ does with the default BLANK='NULL':
+// blanks are ignored, an all-blank field is zero, the exponent may be written
+// with E, D or Q, or as a bare sign ("0.5+02"), and a mantissa without a
+// decimal point carries d implied decimal places.  False when the field is
+// not a number.
+bool parse_fortran_e(const std::string& field, int d, double& v) {
+    std::string t;
+    for (char ch : field)
+        if (ch != ' ' && ch != '\t' && ch != '\r' && ch != '\n') t += ch;
+    if (t.empty()) {
+        v = 0.0;
+        return true;
+    }
+    size_t p = 0;
+    std::string mant;
+    if (t[p] == '+' || t[p] == '-') mant += t[p++];
+    bool digits = false, point = false;
+    for (; p < t.size(); ++p) {
+        const char ch = t[p];
+        if (isdigit((unsigned char)ch)) { mant += ch; digits = true; }
+        else if (ch == '.' && !point) { mant += ch; point = true; }
+        else break;
+    }
+    if (!digits) return false;
+    long ex = 0;
+    if (p < t.size()) {
+        char ch = (char)toupper((unsigned char)t[p]);
+        if (ch == 'E' || ch == 'D' || ch == 'Q') ch = t[++p];
+        if (p >= t.size()) return false;
+        size_t q = p;
+        if (ch == '+' || ch == '-') ++q;
+        if (q >= t.size()) return false;
+        for (size_t r = q; r < t.size(); ++r)
+            if (!isdigit((unsigned char)t[r])) return false;
+        ex = strtol(t.c_str() + p, nullptr, 10);
+    }
+    if (!point) ex -= d;
+    char buf[96];
+    snprintf(buf, sizeof buf, "%sE%ld", mant.c_str(), ex);
+    errno = 0;
+    char* e = nullptr;
+    v = strtod(buf, &e);
+    return e != buf && *e == 0;
 }
 
 // 0-based k range of rank r's restart file.  dnstbl2/originalTBL: istart..iend
@@ -450,6 +499,54 @@ int tbl_statdata_read(const char* path, int32_t nx, int32_t nz, int32_t irec, tb
         st->newk[k] = (int32_t)v[5 * k + 4];
     }
     return TBL_OK;
+}
+
+// The inflow mean profile: 37 records read with FORMAT(24X,E18.8), the value
+// of record 37 kept for every plane above it (dnstbl2/dnstbl.f90:322-345;
+// the same format in originalTBL/fnldnstbl.f90:411-423 and dnssetbl's
+// Input/initProf.dat, dnssetbl/dnssetbl.f90:105-114).  A record shorter than
+// 42 characters is padded with blanks, as a formatted READ pads it.
+int tbl_inflow_profile_read(const char* path, int32_t nz, double* ume1) {
+    if (!path || !ume1 || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string s;
+    if (!read_file(path, s)) return TBL_ERR_IO;
+    double last = 0.0;
+    size_t pos = 0;
+    for (int k = 0; k < TBL_INFLOW_RECORDS; ++k) {
+        if (pos >= s.size()) return TBL_ERR_IO;  // fewer than 37 records
+        size_t e = s.find('\n', pos);
+        if (e == std::string::npos) e = s.size();
+        std::string rec = s.substr(pos, e - pos);
+        pos = e + 1;
+        if (rec.size() < 42) rec.resize(42, ' ');
+        double v = 0.0;
+        if (!parse_fortran_e(rec.substr(24, 18), 8, v)) return TBL_ERR_IO;
+        if (k < nz) ume1[k] = v;
+        last = v;
+    }
+    for (int k = TBL_INFLOW_RECORDS; k < nz; ++k) ume1[k] = last;
+    return TBL_OK;
+}
+
+// The same file from a profile: per record "(1X,I4,1X,E18.8,1X,E18.8)" =
+// k, x3(k) in the 24 skipped columns, then Ume1(k) in E18.8 (9 significant
+// digits) -- the 37 records the reference reads.  Planes above 37 are not
+// written (the reader repeats record 37 there).
+int tbl_inflow_profile_write(const char* path, int32_t nz, const double* x3, const double* ume1) {
+    if (!path || !x3 || !ume1 || nz < TBL_INFLOW_RECORDS) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int k = 0; k < TBL_INFLOW_RECORDS; ++k) {
+        char buf[32];
+        snprintf(buf, sizeof buf, " %4d", k + 1);
+        out += buf;
+        std::string a, b;
+        put_e_wd(a, x3[k], 18, 8);
+        put_e_wd(b, ume1[k], 18, 8);
+        out += a;   // " " + 18 columns: 24 columns in all before the value
+        out += b.substr(1);
+        out += "\n";
+    }
+    return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
 }
 
 }  // extern "C"

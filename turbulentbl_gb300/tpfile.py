@@ -2,7 +2,8 @@
 
 The readers and writers are the C++ ones in libtblgpu.so
 (csrc/tbl_restart.cpp: tbl_tp_write, tbl_tp_write_ranks, tbl_tp_merge,
-tbl_tp_read, tbl_counters_*, tbl_statdata_*); they touch no device.  Formats
+tbl_tp_read, tbl_counters_*, tbl_statdata_*, tbl_inflow_profile_*); they
+touch no device.  Formats
 (``fmt``): 0 dnstbl2's 15 columns (x y z U V W P Um Vm Wm Uf Vf Wf Wt Nk),
 1 originalTBL's 8 (x y z U V W T P), 2 dnssetbl's 7 (x y z U V W P).
 
@@ -38,6 +39,8 @@ def _lib():
             "tbl_counters_read": [S, ip, ip, ip, ip],
             "tbl_statdata_write": [S, I, I, I, Sp],
             "tbl_statdata_read": [S, I, I, I, Sp],
+            "tbl_inflow_profile_read": [S, I, dp],
+            "tbl_inflow_profile_write": [S, I, dp, dp],
         }
         for name, args in sigs.items():
             f = getattr(lib, name)
@@ -157,3 +160,20 @@ def read_statdata(path, st, irec):
     s.usum2, s.vsum2, s.wsum2, s.wt = (abi.dptr(st[n]) for n in ("usum2", "vsum2", "wsum2", "wt"))
     s.newk = abi.iptr(st["newk"])
     _check(_lib().tbl_statdata_read(_b(path), nx, nz, irec, C.byref(s)), "tbl_statdata_read")
+
+
+def read_inflow_profile(path, nz):
+    """The inflow mean profile Ume1 (nz values) from U_innerdns.dat: 37
+    records FORMAT(24X,E18.8), record 37 repeated above plane 37."""
+    u = np.zeros(nz)
+    _check(_lib().tbl_inflow_profile_read(_b(path), nz, abi.dptr(u)), "tbl_inflow_profile_read")
+    return u
+
+
+def write_inflow_profile(path, x3, ume1):
+    """U_innerdns.dat for a profile (nz >= 37): k and x3(k) in the skipped
+    columns, Ume1(k) in E18.8, the 37 records the reference reads."""
+    x3 = np.ascontiguousarray(x3, dtype=np.float64)
+    u = np.ascontiguousarray(ume1, dtype=np.float64)
+    _check(_lib().tbl_inflow_profile_write(_b(path), len(u), abi.dptr(x3), abi.dptr(u)),
+           "tbl_inflow_profile_write")
