@@ -26,7 +26,7 @@ import pytest
 CH = 4     # points per lane and step (CHUNK)
 KG = 4     # planes (warps) per CTA
 RING = 4   # plane-to-plane slots
-NPF = 4    # operand slots
+OPB = 16   # operand buffer elements per lane (position q at q % OPB)
 
 
 def fma(a, b, c):
@@ -188,7 +188,7 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
         maxT = max(maxT, T1)
         st[(cidx, by, wid)] = dict(last=[[0.0] * CH for _ in range(32)], carry=[0.0] * 32,
                                    slots={}, done=-1)
-    # issue_raw bookkeeping: slots[(lane, slot)] = (chunk, step)
+    # issue_raw bookkeeping: slots[(lane, element)] = (chunk, step, position held)
     def chunk_of(inf, lane, ts):
         return (CH * (ts - inf['T0']) - plag * lane + CH - 1) >> 2
 
@@ -203,13 +203,17 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
             if ts <= inf['T1'] and 0 <= ac < inf['Cl']:
                 i0 = CH * (inf['c_hi'] - ac if mode == 2 else inf['c_lo'] + ac)
                 assert i0 % CH == 0 and i0 + CH <= sx
-                st[w]['slots'][(lane, ts % NPF)] = (ac, ts)
+                base = (CH * ac) & (OPB - 1)
+                assert base % CH == 0  # 16-byte aligned destination
+                for t in range(CH):
+                    pos = CH * ac + (CH - 1 - t if mode == 2 else t)
+                    st[w]['slots'][(lane, base + t)] = (ac, ts, pos)
 
     for w in info:
         issue(w, info[w]['T0'])
         issue(w, info[w]['T0'] + 1)
 
-    checks = dict(j_wait=0, k_wait=0)
+    checks = dict(j_wait=0, k_wait=0, fast=0)
     for T in range(0, maxT + 1):
         snapG, snapRH, snapOUT = list(G), list(RH), list(OUT)
         snap_ring = dict(ring)
@@ -265,10 +269,10 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
                     if act[e]:
                         q = qb + e
                         assert 0 <= ix[e] < sx
-                        slot = T % NPF if (q >> 2) == aT else (T + NPF - 1) % NPF
                         assert (q >> 2) in (aT, aT - 1)
-                        ent = st[w]['slots'].get((lane, slot))
-                        assert ent is not None and ent[0] == (q >> 2), ("slot content", ent, q >> 2, T)
+                        el = (q ^ (CH - 1) if mode == 2 else q) & (OPB - 1)
+                        ent = st[w]['slots'].get((lane, el))
+                        assert ent is not None and ent[0] == (q >> 2) and ent[2] == q, ("buffer content", ent, q, T)
                         assert ent[1] <= T
                         r_ = inp[idx(ix[e], j, k)]  # operands are inputs, never overwritten before use
                         if mode == 1:
@@ -277,6 +281,18 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
                         cur[e] = p0 * r_ if mode == 2 else r_
                 lanes.append(dict(lane=lane, jr=jr, line_ok=line_ok, j=j, k=k, jm=jm, jp=jp, kidx=kidx, qb=qb,
                                   act=act, ix=ix, inr=inr, cur=cur, jidx=jidx))
+            # the kernel's specialised step: every lane has a line and all its
+            # points are interior positions of the block, not the first one
+            ibase_w = CH * inf['c_hi'] + CH - 1 if mode == 2 else CH * inf['c_lo']
+            qlo = max(1, ibase_w - (nx - 2) if mode == 2 else 1 - ibase_w)
+            qhi = min(inf['Q'] - 1, ibase_w - 1 if mode == 2 else nx - 2 - ibase_w)
+            q0 = CH * (T - T0)
+            full_warp = plag == 1 and 32 * cta['jb'] + 31 < J
+            if full_warp and q0 - 31 >= qlo and q0 + CH - 1 <= qhi:
+                checks['fast'] += 1
+                for L in lanes:
+                    assert L['line_ok'] and all(L['act']) and all(L['inr'])
+                    assert all(L['qb'] + e != 0 for e in range(CH))
             # pk, pj0, wrap
             for L in lanes:
                 lane = L['lane']
@@ -441,10 +457,23 @@ def test_model_mirrors_the_kernel_source():
         "const int dl = plag * lane;",
         "auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };",
         "const int qb = CH * (T - T0) - dl;",
-        "const int slot = (q >> 2) == aT ? T % NPF : (T + NPF - 1) % NPF;",
-        "const int el = MODE == SW_BWD ? CH - 1 - (q & (CH - 1)) : (q & (CH - 1));",
+        "const Val r = opb[(MODE == SW_BWD ? (q ^ (CH - 1)) : q) & (OPB - 1)];",
+        "Val* dst = opb + ((CH * ac) & (OPB - 1));",
+        "const int qlo = max(1, MODE == SW_BWD ? ibase - (g.nx - 2) : 1 - ibase);",
+        "const int qhi = min(Q - 1, MODE == SW_BWD ? ibase - 1 : g.nx - 2 - ibase);",
+        "const bool full_warp = plag == 1 && 32 * cta.jb + 31 < J;",
+        "const bool ok = (full_warp && q0 - 31 >= qlo && q0 + CH - 1 <= qhi) ? step(T, std::true_type{})",
         "a.plag = h->g.ny - 2 <= 4 ? CHUNK : 1;",
         "constexpr int RING = 4;",
-        "constexpr int NPF = 4;",
+        "constexpr int OPB = 16;",
     ):
         assert line in src, line
+
+
+@pytest.mark.parametrize("mode,nib", [(0, 1), (1, 1), (2, 1), (1, 2), (2, 2)])
+def test_specialised_steps_reproduce_the_sequential_sweep(mode, nib):
+    """Lines long enough that the 32-lane warps run steps with every point
+    interior (the kernel's specialised step), on two full row blocks."""
+    bad, _, checks = run(mode, 83, 64, [5, 4], kernel_plag(64), 0, nib)
+    assert bad == 0
+    assert checks["fast"] > 0

@@ -27,6 +27,7 @@
 //
 // The backward SSOR sweep is the same schedule on mirrored indices.
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "tbl_internal.cuh"
 #include "tbl_kernels.cuh"
@@ -101,8 +102,8 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
 }
 
 constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
-constexpr int NPF = 4;   // operand slots per warp: chunks are copied two steps ahead, and a slot is
-                         // rewritten one step after its last read
+constexpr int OPB = 16;  // operand buffer per lane: position q of the line at element q % OPB; chunks
+                         // are copied two steps ahead, and the live positions span 11 < OPB
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only), its group
 // commit and the wait for all but the most recent N groups.
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
     unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
     __shared__ int s_prog[KG];
     __shared__ __align__(16) Val s_ring[KG][RING][32][CH];
-    __shared__ __align__(16) Val s_pf[KG][NPF][32][CH];
+    __shared__ __align__(16) Val s_op[KG][32][OPB];
     if (lane == 0) s_prog[wid] = -1;
     __syncthreads();
 
@@ -282,19 +283,21 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
 
     // raw operands.  The lane's window of step ts ends in chunk
     // a(ts) = (CH*(ts - T0) - dl + CH-1) / CH of the block (floor); each lane
-    // copies that chunk (32 bytes FP64, 16 bytes FP32) into its shared-memory
-    // slot ts % NPF two steps ahead with cp.async (one commit group per step,
-    // empty when the chunk is outside the block or the lane has no line) and
-    // waits for the group at the top of step ts.  A window that is not
-    // chunk-aligned also reads the previous chunk, still in slot (ts-1) % NPF.
+    // copies that chunk (32 bytes FP64, 16 bytes FP32) with cp.async two steps
+    // ahead into its operand buffer, position q of the block at element
+    // q % OPB (one commit group per step, empty when the chunk is outside the
+    // block or the lane has no line), and waits for the group at the top of
+    // step ts.  The backward sweep's chunk holds its positions in reverse
+    // memory order, so position q sits at element (q ^ 3) % OPB.
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
+    Val* const opb = &s_op[wid][lane][0];
     auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };
     auto issue_raw = [&](int ts) {
         const int ac = chunk_of(ts);
         if (line_ok && ts <= T1 && ac >= 0 && ac < Cl) {
             const int i0 = CH * (MODE == SW_BWD ? c_hi - ac : c_lo + ac);
-            Val* dst = &s_pf[wid][ts % NPF][lane][0];
+            Val* dst = opb + ((CH * ac) & (OPB - 1));
 #pragma unroll
             for (int b = 0; b < (int)(CH * sizeof(Val)) / 16; ++b)
                 cp_async16(dst + b * (16 / sizeof(Val)), inp + i0 + b * (16 / sizeof(Val)));
@@ -306,21 +309,29 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
     issue_raw(T0 + 1);
     Val pj_pf[CH], pk_pf[CH];
     bool pj_ok = false, pk_ok = false;
-    int abort = 0;
 
-    for (int T = T0; T <= T1; ++T) {
+    // Positions a step may take without any point being a boundary or
+    // outside the block: i in 1..nx-2 and q in 1..Q-1.  A step whose 32
+    // lanes all have lines and all lie there (most steps of a long line)
+    // runs the body specialised for it: no per-point predicates.
+    const int qlo = max(1, MODE == SW_BWD ? ibase - (g.nx - 2) : 1 - ibase);
+    const int qhi = min(Q - 1, MODE == SW_BWD ? ibase - 1 : g.nx - 2 - ibase);
+    const bool full_warp = plag == 1 && 32 * cta.jb + 31 < J;
+
+    // One wavefront step; false when a wait timed out (the error word is set).
+    auto step = [&](const int T, auto fast_tag) -> bool {
+        constexpr bool FAST = decltype(fast_tag)::value;
         const int qb = CH * (T - T0) - dl;  // position of point 0
-        const int aT = chunk_of(T);
         int ix[CH];
         bool act[CH], inr[CH];
 #pragma unroll
         for (int e = 0; e < CH; ++e) {
             const int q = qb + e;
-            act[e] = line_ok && q >= 0 && q < Q;
+            act[e] = FAST || (line_ok && q >= 0 && q < Q);
             ix[e] = ibase + idir * q;
-            inr[e] = ix[e] >= 1 && ix[e] <= g.nx - 2;
+            inr[e] = FAST || (ix[e] >= 1 && ix[e] <= g.nx - 2);
         }
-        // this step's operands, read from the shared-memory slots and scaled
+        // this step's operands, read from the operand buffer and scaled
         // before the warp waits for its producers.  A register prefetch a
         // step ahead was slower (loads still in flight at the end-of-step
         // release have to complete first); cp.async copies are not ordered
@@ -332,13 +343,12 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
             cur[e] = Val(0);
             if (act[e]) {
                 const int q = qb + e;
-                const int slot = (q >> 2) == aT ? T % NPF : (T + NPF - 1) % NPF;
-                const int el = MODE == SW_BWD ? CH - 1 - (q & (CH - 1)) : (q & (CH - 1));
-                const Val r = s_pf[wid][slot][lane][el];
+                const Val r = opb[(MODE == SW_BWD ? (q ^ (CH - 1)) : q) & (OPB - 1)];
                 cur[e] = MODE == SW_BWD ? p0 * r : r;
             }
         }
         // ---- wait for the producers of step T-1 (lane 0 for the warp)
+        int abort = 0;
         if (lane == 0) {
             if (fj && T - T0 < Cl && !pj_ok && seen_j < T - 1) {
                 seen_j = wait_global(fj, tag, T - 1);
@@ -354,12 +364,7 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
                 }
             }
         }
-        __syncwarp();
-        if (__shfl_sync(0xffffffffu, abort, 0)) {
-            if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
-            cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
-            return;
-        }
+        if (__shfl_sync(0xffffffffu, abort, 0)) return false;
         // ---- inputs of the plane below (same positions, one step earlier)
         // and of the row above for lane 0 (chunk-aligned: lane 0 lags by 0)
         Val pk[CH], pj0[CH];
@@ -385,22 +390,28 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
         // ---- the points in sweep order: the (j-1) input of point e is the
         // neighbour lane's point e - plag (this step) or e - plag + CH (the
         // step before), by shuffle; lane 0 has it from the row above
+        const int pl = FAST ? 1 : plag;
         Val out[CH];
 #pragma unroll
         for (int e = 0; e < CH; ++e) {
-            const Val src = plag == 1 ? (e == 0 ? last[CH - 1] : out[e > 0 ? e - 1 : 0]) : last[e];
+            const Val src = pl == 1 ? (e == 0 ? last[CH - 1] : out[e > 0 ? e - 1 : 0]) : last[e];
             Val pj = __shfl_up_sync(0xffffffffu, src, 1);
             if (lane == 0) pj = pj0[e];
             const Val nv = fma(cj, pj, cur[e]);
-            out[e] = Val(0);
-            if (act[e]) {
-                if (qb + e == 0) carry = Val(0);  // first position of the block: nothing before it
-                if (inr[e]) {
-                    carry = fma(ci, carry, nv);
-                    out[e] = carry;
-                } else {  // outside 1..nx-2: the GS inflow boundary value, or zero
-                    out[e] = (MODE == SW_GS && ix[e] == 0) ? bnd : Val(0);
-                    carry = out[e];
+            if (FAST) {
+                carry = fma(ci, carry, nv);
+                out[e] = carry;
+            } else {
+                out[e] = Val(0);
+                if (act[e]) {
+                    if (qb + e == 0) carry = Val(0);  // first position of the block: nothing before it
+                    if (inr[e]) {
+                        carry = fma(ci, carry, nv);
+                        out[e] = carry;
+                    } else {  // outside 1..nx-2: the GS inflow boundary value, or zero
+                        out[e] = (MODE == SW_GS && ix[e] == 0) ? bnd : Val(0);
+                        carry = out[e];
+                    }
                 }
             }
         }
@@ -410,12 +421,7 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
         if (has_down) {
             if (lane == 0 && T - RING + 1 >= T0 + 1)
                 if (!wait_cta(&s_prog[wid + 1], min(T - RING + 1, T1 + 1))) abort = 1;
-            __syncwarp();
-            if (__shfl_sync(0xffffffffu, abort, 0)) {
-                if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
-                cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
-                return;
-            }
+            if (__shfl_sync(0xffffffffu, abort, 0)) return false;
             Val* ws = &s_ring[wid][T & (RING - 1)][lane][0];
 #pragma unroll
             for (int e = 0; e < CH; ++e) ws[e] = out[e];
@@ -463,6 +469,18 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
             }
         }
         issue_raw(T + 2);
+        return true;
+    };
+
+    for (int T = T0; T <= T1; ++T) {
+        const int q0 = CH * (T - T0);  // lane 0's first position; lane 31's is q0 - 31
+        const bool ok = (full_warp && q0 - 31 >= qlo && q0 + CH - 1 <= qhi) ? step(T, std::true_type{})
+                                                                             : step(T, std::false_type{});
+        if (!ok) {
+            if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
+            cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
+            return;
+        }
     }
     cp_async_wait<0>();
 }
