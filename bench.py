@@ -225,7 +225,7 @@ def run_gpu(wl, nproc, steps, warmup, world, rank, local, do_e2e, do_cpu, cpu_bu
     clk = clocks.stop()
     launches = g.launches() - launches0
     L.tbl_profile(g._h, 0)
-    groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launch_groups": nl[q]} for q in range(ng - 1)}
+    groups = {GROUP_NAMES[q]: {"ms": ms[q], "bytes": by[q], "launches": nl[q]} for q in range(ng - 1)}
     out = {"elapsed": elapsed, "host_elapsed": e1 - e0, "recs": recs, "status": st_all, "launches": launches,
            "clocks": clk, "groups": groups}
     if (wl.precision == abi.TBL_PREC_MIXED or rb or extra_flags) and do_accuracy:
@@ -290,9 +290,18 @@ def mixed_accuracy(wl, nproc, variant, dm, sm, nsteps, recs):
     prof = lambda u: u[1:-1, 1:-1, :].mean(axis=(0, 1))  # mean over x and span at each wall distance
     p64, pm = prof(d["u"]), prof(dm["u"])
     us64, usm = s64["usum"][1:-1, 1:-1], sm["usum"][1:-1, 1:-1]
+    # per statistic: the running span sums of the means and products, the
+    # rescaling's thicknesses and Re_theta, wall shear and mass flux
+    per_stat = {}
+    for f in list(abi.STATS_FIELDS) + ["deltastar", "theta", "ht", "reth", "tauw_sum", "ubulk"]:
+        a, b = np.asarray(sm[f]), np.asarray(s64[f])
+        n = float(np.linalg.norm(b))
+        per_stat[f] = float(np.linalg.norm(a - b) / n) if n > 0 else float(np.linalg.norm(a))
+    per_stat["lamda03"] = abs(sm["lamda03"] - s64["lamda03"]) / max(abs(s64["lamda03"]), 1e-300)
     return {"steps_compared": nsteps, "rel_l2": rel,
             "mean_profile_max_rel": float(np.abs(pm - p64).max() / np.abs(p64).max()),
             "usum_max_rel": float(np.abs(usm - us64).max() / max(np.abs(us64).max(), 1e-300)),
+            "statistics_rel_l2": per_stat,
             "ppe_rel_resid_max": max(r["ppe_rel_resid"] for r in recs)}
 
 
@@ -383,7 +392,11 @@ def main():
                     help="time the discrete adjoint of a window on the 256x96x96 adjoint workload instead")
     ap.add_argument("--window", type=int, default=50)
     ap.add_argument("--ckpt", type=int, default=10)
-    ap.add_argument("--fd-dirs", type=int, default=4)
+    ap.add_argument("--fd-dirs", type=int, default=16)
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="leave out the mixed-precision arm of the default line")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="leave out the adjoint/forward cost block of the default line")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.adjoint:
@@ -447,13 +460,53 @@ def main():
     if rank != 0:
         return
     K = args.steps
+    line = gpu_line(wl, r, K, world, args.warmup, config)
+    line["metric"] = metric
+    if "cpu" in r:
+        c = r["cpu"]
+        line["cpu_baseline"] = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    # the rest of the headline metric: the mixed-precision step on the same
+    # box against this FP64 step, and the adjoint/forward cost of a window
+    if not args.no_mixed and wl.name == "box512_fp64" and world == 1:
+        wm = WORKLOADS["box512_mixed"]
+        rm = run_gpu(wm, args.nproc, K, max(args.warmup, 3), world, rank, local, False, False, 0.0, True)
+        ml = gpu_line(wm, rm, K, world, args.warmup, dict(config, workload=wm.name))
+        mixed = {k: ml[k] for k in ("value", "unit", "ms_per_step", "roofline", "step_hbm", "groups_ms_per_step",
+                                    "gmres_iters_per_step", "gs_sweeps_per_step", "status", "gpu_launches", "clocks")}
+        mixed["workload"] = wm.name
+        mixed["vs_fp64"] = ml["value"] / line["value"]
+        mixed["ppe_rel_resid_max"] = ml.get("ppe_rel_resid_max")
+        mixed["accuracy_vs_fp64"] = ml.get("accuracy_vs_fp64")
+        mixed["precision"] = ("FP32 fields, stencils and inner GMRES (restart 40, inner tol 1e-5) in FP64 "
+                              "iterative refinement to 1e-10 and a true PPE residual <= 1e-8; FP64 Gram-Schmidt "
+                              "sums, Hessenberg, Givens, recycling and statistics")
+        line["mixed"] = mixed
+    if not args.no_adjoint and wl.name == "box512_fp64" and world == 1:
+        wa = WORKLOADS["box256_adjoint"]
+        ra = run_adjoint(wa, args.nproc, args.window, args.ckpt, args.fd_dirs, local)
+        rep = [x["rel_err"] for x in ra["fd"] if x["branches"] == "replayed"]
+        line["adjoint"] = {
+            "workload": wa.name, "reference_n3d": list(wa.n3d), "window_steps": args.window,
+            "checkpoint_every": args.ckpt, "forward_ms": ra["forward_ms"], "backward_ms": ra["backward_ms"],
+            "ratio": ra["ratio"], "fd_directions": len(rep), "max_fd_rel_err": max(rep or [0.0]),
+            "fd_free_branches_rel_err": [x["rel_err"] for x in ra["fd"] if x["branches"] == "free"],
+            "objective": "mean wall shear over x in [10, 14], window-averaged",
+            "control": "wall-normal blowing on the nx x (ny-2) wall grid, N(0, 1e-3) from seed 3"}
+    print(json.dumps(line), flush=True)
+
+
+def gpu_line(wl, r, K, world, warmup, config):
+    """The JSON line of one GPU arm: whole-job rate, the roofline of the
+    kernel group with the largest share of the step, per-group times."""
     value = whole_job_rate(wl.points, K, world, r["elapsed"])
     hbm, hbm_kind = peaks()
     groups = r["groups"]
     top = max(groups, key=lambda k: groups[k]["ms"])
     tg = groups[top]
-    launches_top = tg["launch_groups"]
-    achieved = tg["bytes"] / (tg["ms"] * 1e-3) / 1e9 if tg["ms"] > 0 else 0.0
+    nl = max(tg["launches"], 1)
+    per_launch_ms = tg["ms"] / nl
+    bytes_per_launch = tg["bytes"] / nl
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9 if tg["ms"] > 0 else 0.0
     tab = traffic_table()
     tt = tab.get(f"{wl.name}/{top}", tab.get(top))
     traffic = tt.get("bytes_per_launch") if isinstance(tt, dict) else tt
@@ -463,10 +516,16 @@ def main():
                 "traffic_note": (f"ncu dram bytes of one {tt['launch']} vs {tt['algorithmic_bytes_per_launch']:.0f} "
                                  f"algorithmic ({tt['source']})") if isinstance(tt, dict) else None,
                 "share_of_step": tg["ms"] / (r["elapsed"] * 1e3),
-                "per_launch_ms": tg["ms"] / max(launches_top, 1)}
+                "launches": tg["launches"], "per_launch_ms": per_launch_ms,
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "dram_gbs": (traffic / (per_launch_ms * 1e-3) / 1e9) if traffic and per_launch_ms > 0 else None,
+                "dram_frac": (traffic / (per_launch_ms * 1e-3) / 1e9 / hbm) if traffic and per_launch_ms > 0 else None,
+                "how": ("algorithmic bytes of the group's launches / their CUDA-event time (events bracket each "
+                        "group of launches on the library's stream), per launch")}
     step_bytes = sum(v["bytes"] for v in groups.values())
-    line = {"metric": metric, "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": K,
-            "warmup": max(args.warmup, 3), "ms_per_step": r["elapsed"] * 1e3 / K, "higher_is_better": True,
+    dtype = "f64" if wl.precision == 0 else "f32+f64"
+    line = {"metric": "Mpt-steps/s", "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": K,
+            "warmup": max(warmup, 3), "ms_per_step": r["elapsed"] * 1e3 / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded 1/7-law + curl noise)",
             "config": config, "roofline": roofline,
             "step_hbm": {"algorithmic_gb_per_step": step_bytes / K / 1e9,
@@ -486,9 +545,7 @@ def main():
         line["ppe_rel_resid_max"] = max(x["ppe_rel_resid"] for x in r["recs"])
     if "accuracy" in r:
         line["accuracy_vs_fp64"] = r["accuracy"]
-    if "cpu" in r:
-        c = r["cpu"]
-        line["cpu_baseline"] = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return line
     print(json.dumps(line), flush=True)
 
 

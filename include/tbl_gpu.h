@@ -228,8 +228,8 @@ int tbl_upload_fields(tbl_handle* h, const double* u, const double* v, const dou
 
 /* Kernel-group timing with CUDA events on the library's stream.  enable=1
  * turns it on (and clears the totals), 0 turns it off.  tbl_profile_read
- * copies per-group totals: milliseconds, algorithmic bytes and launches, for
- * TBL_PROF_NGROUPS groups (indices TBL_PROF_*). */
+ * copies per-group totals: milliseconds, algorithmic bytes and kernel
+ * launches, for TBL_PROF_NGROUPS groups (indices TBL_PROF_*). */
 #define TBL_PROF_CONV      0  /* convection + explicit RHS */
 #define TBL_PROF_GS_SWEEP  1  /* GS wavefront sweeps */
 #define TBL_PROF_GS_RESID  2  /* GS residual checks */

@@ -2,12 +2,25 @@
 quoted on (the parity tests proper at full size).
 
 * The 128 x 64 x 64 box (n3d 128 x 66 x 64, GMRES restart 30, tol 1e-8,
-  P = 8), 200 steps from the seeded perturbed 1/7-law start: every step u, v,
-  w and p within 1e-12 relative L2 of the oracle, with equal Gauss-Seidel
-  sweep and GMRES iteration counts; then the statistics of the run's second
-  half (mean U+ profiles, rms profiles, the Reynolds shear stress u'v', the
-  skin friction Cf(x) and the momentum-thickness Reynolds number Re_theta(x)
-  and its growth from inflow to outflow) within 0.5%.
+  P = 8), 200 steps from the seeded perturbed 1/7-law start with dt from
+  CFL 0.1 and a statistics window of cum = 1000 steps: every step u, v, w and p within
+  1e-12 relative L2 of the oracle, with equal Gauss-Seidel sweep and GMRES
+  iteration counts; then the statistics of the run's second half (mean U+
+  profiles, rms profiles, the Reynolds shear stress u'v', the skin friction
+  Cf(x) and the momentum-thickness Reynolds number Re_theta(x) and its growth
+  from inflow to outflow) within 0.5%, and the library's own running sums
+  within 1e-12.
+* The same box as the parity case states it, dt from CFL 0.3 and dnstbl2's
+  own rescaling every cum = 5 steps.  On this synthetic start (a 1/7 law
+  with noise, not a developed boundary layer) the rescaling factor
+  lamda = u_tau(inflow) / u_tau(recycling plane) (dnstbl2/dnstbl.f90:
+  2152-2156) grows every window, the recycled inflow fluctuations with it,
+  and the run stops on the reference's blow-up test u' > 25 (:1749-1775) at
+  step 72.  (With cum = 1000 the same dt stops at step 143 in the interior:
+  forward-Euler central convection (:621-768) grows its shortest waves at a
+  rate that rises with the CFL number, and Re_theta = 300 on this grid damps
+  them too little; CFL 0.1 runs 200 steps.)  Both codes must take the same
+  steps to the stop and stop at the same step.
 * The 512 x 128 x 128 box (n3d 512 x 130 x 128, restart 40, tol 1e-10,
   P = 8), three steps: fields within 1e-12, counts equal.
 
@@ -16,6 +29,8 @@ after each step (span and time means of the reference's collocated fields,
 dnstbl2/dnstbl.f90:1902-1993 and :2084-2277 for what the reference derives
 from them).
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -89,8 +104,9 @@ def _compare_stats(sg, so, re, stations):
 
 def test_config1_box128_200_steps_match_the_oracle():
     from turbulentbl_gb300.lib import TblGpu
-    wl = WORKLOADS["box128_fp64"]
+    wl = dataclasses.replace(WORKLOADS["box128_fp64"], cfl=0.1)
     mesh, rp, st = make_state(wl, nproc=8)
+    rp.cum = 1000
     o = OracleRunner(mesh, rp)
     g = TblGpu(mesh, rp)
     o.upload(st)
@@ -119,10 +135,41 @@ def test_config1_box128_200_steps_match_the_oracle():
     stats = _compare_stats(sg, so, rp.re, stations=[mesh.nx // 4, mesh.nx // 2, irec])
     for k, v in stats.items():
         assert v <= STAT_TOL, (k, v)
-    # the library's own rescaling outputs (delta*, theta, H, Re_theta) agree too
+    # the library's own running statistics (200 steps of span sums) agree too
     ga, oa = g.download_stats(), o.download_stats()
-    for f in ("deltastar", "theta", "ht", "reth"):
+    assert ga["nstat"] == oa["nstat"] > 0
+    for f in abi.STATS_FIELDS + ["tauw_sum", "ubulk"]:
         assert rel(ga[f], oa[f]) <= 1e-12, f
+    g.close()
+
+
+def test_config1_box128_rescaling_every_5_steps_blows_up_at_the_same_step():
+    from turbulentbl_gb300.lib import TblGpu
+    wl = WORKLOADS["box128_fp64"]
+    mesh, rp, st = make_state(wl, nproc=8)
+    assert rp.cum == 5
+    o = OracleRunner(mesh, rp)
+    g = TblGpu(mesh, rp)
+    o.upload(st)
+    g.upload(st)
+    lam = []
+    for s in range(200):
+        so_st, ro = o.step(1, check=False)
+        sg_st, rg = g.step(1, check=False)
+        assert so_st == sg_st, (s, so_st, sg_st)
+        assert g.last_counts() == o.last_counts(), s
+        lam.append(rg[0]["lamda"])
+        assert rg[0]["lamda"] == pytest.approx(ro[0]["lamda"], rel=1e-12)
+        if s % 10 == 0 and so_st == abi.TBL_OK:
+            a = o.download(fields=("u", "v", "w", "p"))
+            b = g.download(fields=("u", "v", "w", "p"))
+            for f in ("u", "v", "w", "p"):
+                assert rel(b[f], a[f]) <= TOL, (s, f, rel(b[f], a[f]))
+        if so_st != abi.TBL_OK:
+            break
+    assert so_st == abi.TBL_ERR_BLOWUP and s + 1 < 200
+    assert lam[-1] > 1.5 * lam[10]  # the rescaling factor grew window after window
+    g.close()
 
 
 def test_config2_box512_three_steps_match_the_oracle():

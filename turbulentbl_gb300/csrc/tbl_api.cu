@@ -27,7 +27,7 @@ static int take_event(tbl_handle* h) {
     return (int)h->prof_used++;
 }
 
-ProfScope::ProfScope(tbl_handle* h_, int g_, double b_) : h(h_), group(g_), bytes(b_), e0(-1) {
+ProfScope::ProfScope(tbl_handle* h_, int g_, double b_) : h(h_), group(g_), bytes(b_), e0(-1), l0(h_->launches) {
     if (!h->prof_on) return;
     e0 = take_event(h);
     if (e0 >= 0) cudaEventRecord(h->prof_ev[e0], h->stream);
@@ -38,7 +38,7 @@ ProfScope::~ProfScope() {
     int e1 = take_event(h);
     if (e1 < 0) return;
     cudaEventRecord(h->prof_ev[e1], h->stream);
-    h->prof_marks.push_back({group, e0, e1, bytes});
+    h->prof_marks.push_back({group, e0, e1, bytes, h->launches - l0});
 }
 
 // Accumulates the recorded event pairs (the stream must be idle).
@@ -48,7 +48,7 @@ int prof_drain(tbl_handle* h) {
         TBL_CUDA_TRY(cudaEventElapsedTime(&ms, h->prof_ev[m.e0], h->prof_ev[m.e1]));
         h->prof_ms[m.group] += ms;
         h->prof_bytes[m.group] += m.bytes;
-        h->prof_n[m.group] += 1;
+        h->prof_n[m.group] += m.launches;
     }
     h->prof_marks.clear();
     h->prof_used = 0;
@@ -833,6 +833,7 @@ int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
     cudaEvent_t a, b;
     TBL_CUDA_TRY(cudaEventCreate(&a));
     TBL_CUDA_TRY(cudaEventCreate(&b));
+    const int64_t l0 = h->launches;
     TBL_CUDA_TRY(cudaEventRecord(a, h->stream));
     int last = step_loop(h, nsteps, stats);
     TBL_CUDA_TRY(cudaEventRecord(b, h->stream));
@@ -840,7 +841,7 @@ int tbl_step(tbl_handle* h, int32_t nsteps, tbl_step_stats* stats) {
     float ms = 0.f;
     TBL_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
     h->prof_ms[TBL_PROF_TOTAL] += ms;
-    h->prof_n[TBL_PROF_TOTAL] += nsteps;
+    h->prof_n[TBL_PROF_TOTAL] += h->launches - l0;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     return last;

@@ -174,7 +174,7 @@ struct tbl_handle {
     tbl::AdjTape* adj;
     std::vector<double> x1h;  // host copy of x1
     // kernel-group timing (tbl_profile)
-    struct ProfMark { int group; int e0, e1; double bytes; };
+    struct ProfMark { int group; int e0, e1; double bytes; int64_t launches; };
     bool prof_on;
     std::vector<cudaEvent_t> prof_ev;
     size_t prof_used;
@@ -191,6 +191,7 @@ struct ProfScope {
     int group;
     double bytes;
     int e0;
+    int64_t l0;  // h->launches when the scope opened
     ProfScope(tbl_handle* h_, int g_, double b_);
     ~ProfScope();
 };
