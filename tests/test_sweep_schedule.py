@@ -23,22 +23,23 @@ import random
 
 import pytest
 
-CH = 4     # points per lane and step (CHUNK)
+CH = 4     # points per lane and step in FP64 (8 in FP32: run(..., ch=8))
 KG = 4     # planes (warps) per CTA
 RING = 4   # plane-to-plane slots
-OPB = 16   # operand buffer elements per lane (position q at q % OPB)
+OPB = 16   # operand buffer elements per lane, 4 CH (position q at q % OPB)
 
 
 def fma(a, b, c):
     return a * b + c
 
 
-def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
+def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4):
     """One sweep of mode 0 (Gauss-Seidel), 1 (forward SSOR) or 2 (backward
     SSOR) over slabs of K_list planes, J span rows and nx points per line,
     by the kernel's schedule with row lag plag (and block lag changed by
     blag_delta) and sequentially.  Returns (points that differ, last step,
-    counts of the waits checked)."""
+    counts of the waits checked).  ch: points per lane and step."""
+    CH, OPB = ch, 4 * ch
     rnd = random.Random(seed)
     sx = ((nx + 7) + 7) // 8 * 8
     C = (nx - 2) // CH + 1
@@ -190,7 +191,7 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
                                    slots={}, done=-1)
     # issue_raw bookkeeping: slots[(lane, element)] = (chunk, step, position held)
     def chunk_of(inf, lane, ts):
-        return (CH * (ts - inf['T0']) - plag * lane + CH - 1) >> 2
+        return (CH * (ts - inf['T0']) - plag * lane + CH - 1) // CH
 
     def issue(w, ts):
         inf = info[w]
@@ -269,10 +270,10 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
                     if act[e]:
                         q = qb + e
                         assert 0 <= ix[e] < sx
-                        assert (q >> 2) in (aT, aT - 1)
+                        assert (q // CH) in (aT, aT - 1)
                         el = (q ^ (CH - 1) if mode == 2 else q) & (OPB - 1)
                         ent = st[w]['slots'].get((lane, el))
-                        assert ent is not None and ent[0] == (q >> 2) and ent[2] == q, ("buffer content", ent, q, T)
+                        assert ent is not None and ent[0] == (q // CH) and ent[2] == q, ("buffer content", ent, q, T)
                         assert ent[1] <= T
                         r_ = inp[idx(ix[e], j, k)]  # operands are inputs, never overwritten before use
                         if mode == 1:
@@ -399,9 +400,11 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0):
     return bad, maxT, checks
 
 
-def kernel_plag(J):
-    """The row lag the host picks for a grid with J span rows (base_args)."""
-    return CH if J <= 4 else 1
+def kernel_plag(J, ch=CH):
+    """The row lag the host picks for a grid with J span rows (base_args):
+    one position, or a whole chunk when J <= ch (the Gauss-Seidel wrap row
+    would otherwise read row 1's value in the step that writes it)."""
+    return ch if J <= ch else 1
 
 
 def _cases():
@@ -455,7 +458,9 @@ def test_model_mirrors_the_kernel_source():
         "const int T0 = kl + blag * bj;",
         "const int T1 = T0 + (Q - 1 + plag * lane_last) / CH;",
         "const int dl = plag * lane;",
-        "auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };",
+        "auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> LG; };",
+        "template <typename Val> constexpr int sweep_ch() { return sizeof(Val) == 4 ? 8 : 4; }",
+        "constexpr int OPB = 4 * CH;",
         "const int qb = CH * (T - T0) - dl;",
         "const Val r = opb[(MODE == SW_BWD ? (q ^ (CH - 1)) : q) & (OPB - 1)];",
         "Val* dst = opb + ((CH * ac) & (OPB - 1));",
@@ -463,9 +468,9 @@ def test_model_mirrors_the_kernel_source():
         "const int qhi = min(Q - 1, MODE == SW_BWD ? ibase - 1 : g.nx - 2 - ibase);",
         "const bool full_warp = plag == 1 && 32 * cta.jb + 31 < J;",
         "const bool ok = (full_warp && q0 - 31 >= qlo && q0 + CH - 1 <= qhi) ? step(T, std::true_type{})",
-        "a.plag = h->g.ny - 2 <= 4 ? CHUNK : 1;",
+        "a.plag = h->g.ny - 2 <= sweep_ch<T>() ? sweep_ch<T>() : 1;",
         "constexpr int RING = 4;",
-        "constexpr int OPB = 16;",
+
     ):
         assert line in src, line
 
@@ -477,3 +482,32 @@ def test_specialised_steps_reproduce_the_sequential_sweep(mode, nib):
     bad, _, checks = run(mode, 83, 64, [5, 4], kernel_plag(64), 0, nib)
     assert bad == 0
     assert checks["fast"] > 0
+
+
+def _cases8():
+    out = []
+    for mode in (0, 1, 2):
+        for nx, J, Ks, nib in [(83, 64, (5, 4), 1), (40, 33, (3, 6), 1), (83, 64, (5, 4), 2), (17, 5, (3,), 1),
+                               (23, 40, (2, 6, 5), 1), (30, 9, (4,), 1), (21, 8, (3, 2), 1), (150, 40, (5,), 1)]:
+            if mode == 0 and nib > 1:
+                continue
+            out.append((mode, nx, J, Ks, nib))
+    return out
+
+
+@pytest.mark.parametrize("mode,nx,J,Ks,nib", _cases8())
+def test_eight_point_steps_reproduce_the_sequential_sweep(mode, nx, J, Ks, nib):
+    """The FP32 sweeps' 8 points per lane and step, with the row lag the host
+    picks for them (a whole chunk up to 8 span rows)."""
+    bad, _, checks = run(mode, nx, J, list(Ks), kernel_plag(J, 8), 0, nib, ch=8)
+    assert bad == 0
+    if nx > 70 and J >= 32 and nib == 1:
+        assert checks["fast"] > 0
+
+
+def test_one_position_lag_needs_more_rows_than_points_per_step():
+    """With 8 points per step the Gauss-Seidel wrap breaks up to 8 span rows
+    under a one-position lag, and holds from 9."""
+    assert run(0, 23, 8, [3, 4], 1, ch=8)[0] > 0
+    assert run(0, 23, 8, [3, 4], 8, ch=8)[0] == 0
+    assert run(0, 23, 9, [3, 4], 1, ch=8)[0] == 0

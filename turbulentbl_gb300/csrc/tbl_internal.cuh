@@ -25,7 +25,6 @@ namespace tbl {
 
 void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
 
-constexpr int CHUNK = 4;          // i-points per lane per wavefront step
 constexpr int KG = 4;             // k-planes (warps) per wavefront CTA
 constexpr int SSOR_MAX_NIB = 4;    // streamwise SSOR blocks per line at most
 constexpr int RED_THREADS = 256;  // threads per reduction block

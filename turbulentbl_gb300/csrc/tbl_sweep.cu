@@ -9,7 +9,7 @@
 // the same arithmetic per point.  The schedule used here:
 //
 //   * every (j,k) line of a slab is owned by one lane; a lane updates
-//     CHUNK=4 consecutive points of its line per step;
+//     CH consecutive points of its line per step (4 in FP64, 8 in FP32);
 //   * a warp holds 32 consecutive rows of one plane, a CTA holds KG planes;
 //     point i of row j is updated one position after point i of row j-1 (the
 //     value comes from the neighbouring lane by shuffle, within the step or
@@ -59,7 +59,7 @@ struct SweepArgs {
     double omega, sw;           // w, (2-w)/w
     int jb_rows;                // SSOR: rows per span block (a multiple of 32; 0 = one block per slab)
     int nib;                    // SSOR: streamwise blocks (grid.y), 1 = one block per line
-    int plag;                   // positions a row lags the row above: 1, or CHUNK (see base_args)
+    int plag;                   // positions a row lags the row above: 1, or CH (see base_args)
     const T* X;                 // matvec input (FWD) / PCorr (FWD residual mode)
     const double* Q8;           // residual mode when non-null
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
@@ -102,8 +102,19 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
 }
 
 constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
-constexpr int OPB = 16;  // operand buffer per lane: position q of the line at element q % OPB; chunks
-                         // are copied two steps ahead, and the live positions span 11 < OPB
+// Points per lane per step: 4 in FP64 (one 32-byte sector), 8 in FP32.  An
+// FP64 step is bound by its chain of dependent FP64 FMAs (GB300 issues FP64
+// at 1/64 of the FP32 rate), an FP32 step by its fixed synchronisation cost,
+// which 8 points amortise over twice the work (measured at 512 x 130 x 128:
+// FP32 sweeps 185 -> 159 ms a step; 8-point FP64 sweeps and 16-point FP32
+// sweeps were slower).  Each lane's operand buffer holds 4 CH positions:
+// position q of the line at element q % (4 CH); chunks are copied two steps
+// ahead, so the live positions span 3 CH - 1 < 4 CH.
+template <typename Val> constexpr int sweep_ch() { return sizeof(Val) == 4 ? 8 : 4; }
+// Dynamic shared memory of a sweep CTA: the plane-to-plane ring and the operand buffers.
+template <typename Val> constexpr size_t sweep_smem() {
+    return sizeof(Val) * KG * (RING * 32 * sweep_ch<Val>() + 32 * 4 * sweep_ch<Val>());
+}
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only), its group
 // commit and the wait for all but the most recent N groups.
@@ -154,13 +165,15 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // its producers; the (k-1) values of the plane below come through a shared
 // memory ring (RING steps deep, with back-pressure), the (j-1) values of the
 // row above by shuffle within the step or, for lane 0, from global memory.
-// FP32 sweeps keep 6 CTAs per SM (80 registers), FP64 ones 4, so that the
-// Gauss-Seidel sweeps of two velocity components stay co-resident on large
-// grids.
+// Both precisions keep 4 CTAs per SM (at most 128 registers; 64 KB of shared
+// memory in FP64 and 32 KB in FP32), so that the Gauss-Seidel sweeps of the
+// three velocity components stay co-resident at 512 x 130 x 128.
 template <int MODE, typename Val>
-__global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(SweepArgs<Val> a) {
-    constexpr int CH = 4;  // points per lane per step (one 32-byte sector in FP64)
-    static_assert(CH == CHUNK && CH == 4, "positions map to chunks by shifts");
+__global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
+    constexpr int CH = sweep_ch<Val>();
+    constexpr int OPB = 4 * CH;
+    constexpr int LG = CH == 8 ? 3 : 2;  // log2(CH)
+    static_assert(CH == (1 << LG), "positions map to chunks by shifts");
     const Geom& g = a.g;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const SweepCta cta = a.ctas[blockIdx.x];
@@ -179,8 +192,9 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
     const int comp = MODE == SW_GS ? a.comp[compi] : 0;
     unsigned long long* flags = a.flags + (size_t)compi * a.n_cta * KG;
     __shared__ int s_prog[KG];
-    __shared__ __align__(16) Val s_ring[KG][RING][32][CH];
-    __shared__ __align__(16) Val s_op[KG][32][OPB];
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    Val (*s_ring)[RING][32][CH] = reinterpret_cast<Val (*)[RING][32][CH]>(s_dyn);
+    Val (*s_op)[32][OPB] = reinterpret_cast<Val (*)[32][OPB]>(s_dyn + sizeof(Val) * KG * RING * 32 * CH);
     if (lane == 0) s_prog[wid] = -1;
     __syncthreads();
 
@@ -292,7 +306,7 @@ __global__ void __launch_bounds__(KG * 32, sizeof(Val) == 4 ? 6 : 4) k_sweep(Swe
     // GS: the old-value terms come precomputed (k_gs_pre); FWD: r comes
     // pre-scaled by -w/Ap (k_lap); BWD: scaled here.
     Val* const opb = &s_op[wid][lane][0];
-    auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> 2; };
+    auto chunk_of = [&](int ts) { return (CH * (ts - T0) - dl + CH - 1) >> LG; };
     auto issue_raw = [&](int ts) {
         const int ac = chunk_of(ts);
         if (line_ok && ts <= T1 && ac >= 0 && ac < Cl) {
@@ -727,7 +741,7 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     a.slabs = h->slabs;
     a.n_cta = h->n_cta;
     a.P = h->P;
-    a.C = (h->g.nx - 2) / CHUNK + 1;
+    a.C = (h->g.nx - 2) / sweep_ch<T>() + 1;
     a.flags = h->flags;
     a.epoch = h->epoch++;
     a.err = h->err;
@@ -741,7 +755,7 @@ static SweepArgs<T> base_args(tbl_handle* h) {
     // A row lags the row above by one position.  With 4 span rows or fewer the
     // Gauss-Seidel wrap row (which reads row 1's new values from global
     // memory) would share a step with row 1, so those grids lag by a chunk.
-    a.plag = h->g.ny - 2 <= 4 ? CHUNK : 1;
+    a.plag = h->g.ny - 2 <= sweep_ch<T>() ? sweep_ch<T>() : 1;
     a.t = -h->cfg.dt / (h->cfg.re);
     return a;
 }
@@ -750,7 +764,9 @@ template <int MODE, typename T>
 static int launch_sweep(tbl_handle* h, SweepArgs<T>& a, int ncomp) {
     void* args[] = {&a};
     dim3 grid(h->n_cta, ncomp), block(KG * 32);
-    TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE, T>, grid, block, args, 0, h->stream));
+    // (the dynamic shared memory limit of the three sweep kernels of the
+    // handle's precision is raised once, in check_cooperative)
+    TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE, T>, grid, block, args, sweep_smem<T>(), h->stream));
     h->launches++;
     return TBL_OK;
 }
@@ -946,7 +962,9 @@ int check_cooperative(tbl_handle* h) {
     long long cap[3];
     for (int q = 0; q < 3; ++q) {
         int per_sm = 0;
-        TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks[q], KG * 32, 0));
+        const size_t smem = mx ? sweep_smem<float>() : sweep_smem<double>();
+        TBL_CUDA_TRY(cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        TBL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks[q], KG * 32, smem));
         cap[q] = (long long)per_sm * sms;
     }
     h->coop_ok = coop && cap[0] >= h->n_cta && cap[1] >= h->n_cta && cap[2] >= h->n_cta;
@@ -958,7 +976,7 @@ int check_cooperative(tbl_handle* h) {
         const long long fit = (cap[1] < cap[2] ? cap[1] : cap[2]) / (h->n_cta > 0 ? h->n_cta : 1);
         int nib = (int)(fit < SSOR_MAX_NIB ? (fit < 1 ? 1 : fit) : SSOR_MAX_NIB);
         // no empty block: the sweep splits C chunks into blocks of ceil(C/nib)
-        const int C = (h->g.nx - 2) / 4 + 1;
+        const int C = (h->g.nx - 2) / (mx ? sweep_ch<float>() : sweep_ch<double>()) + 1;
         if (nib > C) nib = C;
         const int cb = (C + nib - 1) / nib;
         h->ssor_nib = (C + cb - 1) / cb;
