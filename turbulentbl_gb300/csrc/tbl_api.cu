@@ -300,6 +300,13 @@ int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok)
     double sumnor[3] = {0, 0, 0}, sumav[3] = {0, 0, 0};
     int parity = 0;
     const bool mixed = h->cfg.precision == TBL_PREC_MIXED;
+    // Mixed precision: the increment D of the delta form restarts from zero
+    // (r -= A D in FP64, U += D) each time the residual has fallen 100-fold
+    // since its last start, so that D stays within two orders of magnitude of
+    // the residual it corrects and FP32 rounding of D does not floor the
+    // residual ratio above errorstop (it did at 1024 x 258 x 192).
+    constexpr double kRestartDrop = 1e-2;
+    double restart_at[3] = {1.0, 1.0, 1.0};
     if (mixed)
         for (int c = 0; c < 3; ++c) TRY(launch_gs_delta_init(h, c));
     TRY(launch_halo_init(h, parity));
@@ -316,6 +323,7 @@ int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok)
             TRY(readback(h, &h->sc->red[0], 3 * sizeof(double)));
             const double* red = h->hpin;
             int m = 0;
+            bool restarted = false;
             for (int q = 0; q < n; ++q) {
                 int c = comps[q];
                 double diver = red[c];
@@ -331,11 +339,20 @@ int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok)
                 bool stop = target ? (sweeps[c] >= target[c])
                                    : (sumav[c] < h->cfg.errorstop ||
                                       (h->cfg.variant == TBL_VARIANT_DNSSETBL && diver < (double)1e-12f));
-                if (stop) active[c] = false;
-                else comps[m++] = c;
+                if (stop) {
+                    active[c] = false;
+                    continue;
+                }
+                comps[m++] = c;
+                if (mixed && sumav[c] <= kRestartDrop * restart_at[c]) {
+                    TRY(launch_gs_delta_restart(h, c));
+                    restart_at[c] = sumav[c];
+                    restarted = true;
+                }
             }
             n = m;
             if (n == 0) break;
+            if (restarted) TRY(launch_halo_init(h, parity));  // the restarted increments' halo planes are 0
         }
         {
             ProfScope ps(h, TBL_PROF_GS_SWEEP, 3.0 * 8.0 * h->npts * n);

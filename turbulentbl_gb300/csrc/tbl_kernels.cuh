@@ -19,6 +19,7 @@ int launch_stats(tbl_handle* h);
 int launch_rescale(tbl_handle* h);
 int launch_gs_delta_init(tbl_handle* h, int comp);
 int launch_gs_delta_apply(tbl_handle* h, int comp);
+int launch_gs_delta_restart(tbl_handle* h, int comp);
 
 // tbl_sweep.cu
 int build_sweep_ctas(tbl_handle* h);

@@ -341,20 +341,43 @@ __device__ __forceinline__ float dot4f(float4 a, float4 b) {
     return fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
 }
 
+// Warp sum of 16 FP64 values per lane, as a reduce-scatter: at each of the
+// offsets 16, 8, 4, 2 a lane keeps half of its values, sends the other half to
+// lane ^ offset and adds what it receives; a last exchange with lane ^ 1
+// completes the sums.  Lane l then holds the warp total of value l >> 1: 16
+// FP64 additions per lane instead of the 80 of 16 shuffle trees (FP64 runs at
+// 1/64 of the FP32 rate on this GPU).  Fixed order: deterministic.
+__device__ __forceinline__ double warp_reduce_scatter16(double (&a)[16]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int half = 8; half >= 1; half >>= 1) {
+        const bool up = (lane & (2 * half)) != 0;  // keeps the upper half of the current values
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const double keep = up ? a[i + half] : a[i];
+            const double send = up ? a[i] : a[i + half];
+            a[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2 * half);
+        }
+    }
+    return a[0] + __shfl_xor_sync(0xffffffffu, a[0], 1);
+}
+
 // d[i] = <v_i, w>, g[i] = <v_i, v_{nv-1}> for the G basis vectors of group
-// blockIdx.y (first vector g0 + G*blockIdx.y).  Each thread sums its FP32
-// products over its share of the points (a few float4 at most); the block
-// sums its 2G values with an FP32 shuffle tree per warp and FP64 over the
-// warps, and writes 2G partials.  k_lsg_reduce then sums each value's
-// partials in FP64 (fixed order: deterministic).  Finishing in the last
-// block (a fence, an atomic, then the 2G sums) and FP64 shuffle trees cost
-// as much as the pass's loads.
+// blockIdx.y (first vector g0 + G*blockIdx.y).  The products are FP32 (the
+// vectors are); each thread sums its share (about 16 float4 loads, 64
+// products) in FP32, and from these per-thread partials on every sum is FP64:
+// the warp's, the block's and k_lsg_reduce's (each value's block partials,
+// fixed order).  An FP64 sum per float4 instead cost the mixed step 14 ms at
+// 512 x 130 x 128 (22% of its Gram-Schmidt time).  (Finishing in
+// the last block -- a fence, an atomic, then the 2G sums -- cost as much as
+// the pass's loads, hence the separate reduction.)
 template <int G>
 __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
                                                             const float4* __restrict__ V, long long vstride4, int nv,
                                                             int g0, double* __restrict__ partial, int max_blocks) {
+    static_assert(2 * G <= 16, "the warp reduce-scatter takes 16 values");
     constexpr int NW = RED_THREADS / 32;
-    __shared__ float s_red[2 * G * NW];
+    __shared__ double s_red[16 * NW];
     const int grp = g0 / LSG_G + blockIdx.y;  // slot index of this group
     const int i0 = g0 + blockIdx.y * G;
     const float4* vl = V + (long long)(nv - 1) * vstride4;
@@ -371,19 +394,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
             fg[e] += dot4f(v, l);
         }
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double acc[16];
 #pragma unroll
-    for (int e = 0; e < G; ++e) {
-        const float a = warp_sum(fd[e]), b = warp_sum(fg[e]);
-        if (lane == 0) {
-            s_red[(2 * e) * NW + wid] = a;
-            s_red[(2 * e + 1) * NW + wid] = b;
-        }
-    }
+    for (int e = 0; e < 16; ++e) acc[e] = e < 2 * G ? (double)(e % 2 == 0 ? fd[e / 2] : fg[e / 2]) : 0.0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double tot = warp_reduce_scatter16(acc);  // value lane >> 1
+    if ((lane & 1) == 0) s_red[(lane >> 1) * NW + wid] = tot;
     __syncthreads();
     if (threadIdx.x < 2 * G) {
         double a = 0.0;
-        for (int q = 0; q < NW; ++q) a += (double)s_red[threadIdx.x * NW + q];
+        for (int k = 0; k < NW; ++k) a += s_red[threadIdx.x * NW + k];
         partial[((size_t)grp * 2 * LSG_G + threadIdx.x) * max_blocks + blockIdx.x] = a;
     }
 }

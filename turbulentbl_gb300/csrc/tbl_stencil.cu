@@ -879,8 +879,13 @@ int launch_gs_resid(tbl_handle* h, const int* comps, int ncomp, int nblocks) {
     return TBL_OK;
 }
 
-// Mixed precision: r0 = Q - (I + t L7) U in place of Q, D = 0 (start of the
-// delta-form GS; same iterates as GS on U from U^n, rounding on the small D).
+// Mixed precision, delta form of the Gauss-Seidel solve of (I + t L7) U = Q:
+// the FP32 sweeps iterate on an increment D with right-hand side r = Q - A U.
+// In exact arithmetic U + D are the reference's iterates (a sweep is affine),
+// at every restart of the increment too.  The residuals are formed in FP64
+// from the FP32 data and rounded once, so r carries no FP32 cancellation.
+//
+// Start: r0 = Q - A U in place of Q, D = 0.
 __global__ void __launch_bounds__(128) k_gs_delta_init(Geom g, double t, double aw, double as,
                                                        const double* __restrict__ Ab, const double* __restrict__ At,
                                                        const double* __restrict__ Ap, const float* __restrict__ U,
@@ -889,21 +894,40 @@ __global__ void __launch_bounds__(128) k_gs_delta_init(Geom g, double t, double 
     int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
     long long p = idx(g, i, j, k);
-    const float d = (float)(1.0 + t * Ap[k]), cE = (float)(t * aw), cN = (float)(t * as);
-    const float cT = (float)(t * At[k]), cB = (float)(t * Ab[k]);
-    float r = Q[p] - d * U[p] - cE * U[p + 1] - cE * U[p - 1] - cN * U[idx(g, i, jp1(g, j), k)] -
-              cN * U[idx(g, i, jm1(g, j), k)] - cT * U[p + g.ps] - cB * U[p - g.ps];
-    Q[p] = r;
+    const double d = 1.0 + t * Ap[k], cE = t * aw, cN = t * as, cT = t * At[k], cB = t * Ab[k];
+    const double r = (double)Q[p] - d * (double)U[p] - cE * (double)U[p + 1] - cE * (double)U[p - 1] -
+                     cN * (double)U[idx(g, i, jp1(g, j), k)] - cN * (double)U[idx(g, i, jm1(g, j), k)] -
+                     cT * (double)U[p + g.ps] - cB * (double)U[p - g.ps];
+    Q[p] = (float)r;
     D[p] = 0.0f;
 }
 
-// U += D on the interior (end of the delta-form GS)
-__global__ void __launch_bounds__(128) k_gs_delta_apply(Geom g, const float* __restrict__ D, float* __restrict__ U) {
+// Restart of the increment, first half: r -= A D (the residual of U + D).
+__global__ void __launch_bounds__(128) k_gs_delta_rhs(Geom g, double t, double aw, double as,
+                                                      const double* __restrict__ Ab, const double* __restrict__ At,
+                                                      const double* __restrict__ Ap, const float* __restrict__ D,
+                                                      float* __restrict__ Q) {
+    int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+    if (i > g.nx - 2) return;
+    long long p = idx(g, i, j, k);
+    const double d = 1.0 + t * Ap[k], cE = t * aw, cN = t * as, cT = t * At[k], cB = t * Ab[k];
+    const double r = (double)Q[p] - d * (double)D[p] - cE * (double)D[p + 1] - cE * (double)D[p - 1] -
+                     cN * (double)D[idx(g, i, jp1(g, j), k)] - cN * (double)D[idx(g, i, jm1(g, j), k)] -
+                     cT * (double)D[p + g.ps] - cB * (double)D[p - g.ps];
+    Q[p] = (float)r;
+}
+
+// U += D on the interior (end of the delta-form GS); with zero_d the increment
+// restarts from 0 (second half of a restart).
+__global__ void __launch_bounds__(128) k_gs_delta_apply(Geom g, float* __restrict__ D, float* __restrict__ U,
+                                                        int zero_d) {
     int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
     long long p = idx(g, i, j, k);
     U[p] = U[p] + D[p];
+    if (zero_d) D[p] = 0.0f;
 }
 
 int launch_gs_delta_init(tbl_handle* h, int comp) {
@@ -917,8 +941,20 @@ int launch_gs_delta_init(tbl_handle* h, int comp) {
 }
 
 int launch_gs_delta_apply(tbl_handle* h, int comp) {
-    k_gs_delta_apply<<<interior_grid(h->g), 128, 0, h->stream>>>(h->g, h->Df[comp], h->Uf[comp]);
+    k_gs_delta_apply<<<interior_grid(h->g), 128, 0, h->stream>>>(h->g, h->Df[comp], h->Uf[comp], 0);
     LAUNCH_COUNT(h);
+    return TBL_OK;
+}
+
+// Restart of the increment of one component: r -= A D, U += D, D = 0.
+int launch_gs_delta_restart(tbl_handle* h, int comp) {
+    const Geom& g = h->g;
+    const double t = -h->cfg.dt / (h->cfg.re);
+    k_gs_delta_rhs<<<interior_grid(g), 128, 0, h->stream>>>(g, t, 1.0 / (h->cfg.dx * h->cfg.dx),
+                                                           1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap,
+                                                           h->Df[comp], h->Qf[comp]);
+    k_gs_delta_apply<<<interior_grid(g), 128, 0, h->stream>>>(g, h->Df[comp], h->Uf[comp], 1);
+    h->launches += 2;
     return TBL_OK;
 }
 
