@@ -127,6 +127,8 @@ static void free_all(tbl_handle* h) {
     if (h->AbT) cudaFree(h->AbT);
     if (h->AtT) cudaFree(h->AtT);
     if (h->hpin) cudaFreeHost(h->hpin);
+    for (cudaEvent_t e : h->ahead_ev)
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
@@ -184,6 +186,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
         TBL_CUDA_TRY(cudaDeviceGetAttribute(&h->n_sm, cudaDevAttrMultiProcessorCount, dev));
     }
     TBL_CUDA_TRY(cudaMallocHost(&h->hpin, 4096));
+    for (cudaEvent_t& e : h->ahead_ev) TBL_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     const size_t vol = (size_t)g.vol, n2 = (size_t)nx * nz, pl = (size_t)ny * nz;
     TRY(dalloc(&h->PC, vol));
     TRY(dalloc(&h->Q8, vol));
@@ -367,6 +370,44 @@ int gs_solve(tbl_handle* h, const int* target, tbl_step_stats& st, bool zero_ok)
     return TBL_OK;
 }
 
+// ------------------------------------- Arnoldi steps enqueued one step ahead
+// The host enqueues Arnoldi step k+1 before it waits for step k's residual
+// estimate (an asynchronous copy and an event per step), so the device never
+// idles while the host decides whether the cycle goes on.  Step k's Givens
+// kernel sets sc->stop when the estimate reaches stop_at -- the host's own
+// test, on the same double -- and every kernel of step k+1 then returns at
+// once.  The iteration counts are those of the step-by-step loop
+// (:1187-1188).  Returns the last step taken in kit and its estimate in
+// sumav; the bytes of a step that did nothing are removed from the profile.
+template <typename Step>
+static int arnoldi_ahead(tbl_handle* h, int kmax, double stop_at, Step& step, int& kit, double& sumav) {
+    const int* skip = &h->sc->stop;
+    auto post = [&](int k) -> int {
+        TBL_CUDA_TRY(cudaMemcpyAsync(h->hpin + 64 + (k & 1), &h->sc->sumav, sizeof(double), cudaMemcpyDeviceToHost,
+                                     h->stream));
+        TBL_CUDA_TRY(cudaEventRecord(h->ahead_ev[k & 1], h->stream));
+        return TBL_OK;
+    };
+    TRY(step(1, skip));
+    TRY(post(1));
+    for (int k = 1;; ++k) {
+        const size_t mark0 = h->prof_marks.size();
+        const bool more = k < kmax;
+        if (more) {
+            TRY(step(k + 1, skip));
+            TRY(post(k + 1));
+        }
+        TBL_CUDA_TRY(cudaEventSynchronize(h->ahead_ev[k & 1]));
+        sumav = h->hpin[64 + (k & 1)];
+        if (!(sumav > stop_at) || !more) {
+            kit = k;
+            if (more)
+                for (size_t q = mark0; q < h->prof_marks.size(); ++q) h->prof_marks[q].bytes = 0.0;
+            return TBL_OK;
+        }
+    }
+}
+
 // ---------------------------------------------- mixed-precision Poisson solve
 // FP64 iterative refinement around FP32 GMRES(mixed_kmax): every outer pass
 // forms r = Q8 - L7 p' in FP64, runs one FP32 Arnoldi cycle with the FP32
@@ -428,34 +469,45 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
             TRY(launch_scale_by_inv_f(h, V0, &h->sc->rho));
         }
         int kit = 0;
-        while (kit < kmax && sumav > target && sumav * sumnor > inner_tol * rho_m) {
-            kit = kit + 1;
-            float* W = h->Vf + (size_t)kit * vol;
+        // the cycle stops when the estimate reaches the pass's target or its
+        // inner tolerance relative to the cycle's start (sumav <= thr)
+        const double thr = std::fmax(target, inner_tol * rho_m / sumnor);
+        auto arnoldi_step = [&](int k, const int* skip) -> int {
+            float* W = h->Vf + (size_t)k * vol;
             {
                 ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN);
-                TRY(launch_ssor_fwd_f(h, h->Vf + (size_t)(kit - 1) * vol, nullptr, nullptr));
+                TRY(launch_ssor_fwd_f(h, h->Vf + (size_t)(k - 1) * vol, nullptr, nullptr, skip));
             }
             {
                 ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
-                TRY(launch_ssor_bwd_f(h, W));
+                TRY(launch_ssor_bwd_f(h, W, skip));
             }
-            double* hcol = h->h + (size_t)K1 * (kit - 1);
+            double* hcol = h->h + (size_t)K1 * (k - 1);
             {
                 // low-synch MGS: one dot pass over the basis (+1 vector per extra group), one update pass
-                const int ngr = (kit + 7) / 8;
-                ProfScope ps(h, TBL_PROF_MGS, ((kit + 2.0 * ngr) + (kit + 2.0)) * wN);
-                TRY(launch_lsg_f(h, W, kit, hcol));
+                const int ngr = (k + 7) / 8;
+                ProfScope ps(h, TBL_PROF_MGS, ((k + 2.0 * ngr) + (k + 2.0)) * wN);
+                TRY(launch_lsg_f(h, W, k, hcol, skip));
             }
             {
                 ProfScope ps(h, TBL_PROF_SMALL, 0.0);
-                TRY(launch_givens_k(h, kit, K1));
+                TRY(launch_givens_k(h, k, K1, skip, thr));
             }
             {
                 ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
-                TRY(launch_scale_by_inv_f(h, W, &h->sc->red[8]));
+                TRY(launch_scale_by_inv_f(h, W, &h->sc->red[8], skip));
             }
-            TRY(readback(h, &h->sc->sumav, sizeof(double)));
-            sumav = h->hpin[0];
+            return TBL_OK;
+        };
+        if (h->cfg.flags & TBL_FLAG_RB_PRECOND) {  // one step at a time, read back after each
+            while (kit < kmax && sumav > thr) {
+                kit = kit + 1;
+                TRY(arnoldi_step(kit, nullptr));
+                TRY(readback(h, &h->sc->sumav, sizeof(double)));
+                sumav = h->hpin[0];
+            }
+        } else if (kmax > 0 && sumav > thr) {
+            TRY(arnoldi_ahead(h, kmax, thr, arnoldi_step, kit, sumav));
         }
         iters += kit;
         kits.push_back(kit);
@@ -525,37 +577,48 @@ int gmres(tbl_handle* h, const int32_t* rec, std::vector<int32_t>& kits, tbl_ste
         }
         int kit = 0;
         const int target = rec ? rec[m] : 0;
-        while (rec ? (kit < target) : ((sumav > h->cfg.errtol) && (kit < kmax))) {
-            kit = kit + 1;
-            double* W = h->V + (size_t)kit * vol;
+        // One Arnoldi step (:1059-1191): preconditioned matvec, MGS, Givens,
+        // normalisation.  With skip, every kernel returns at once when an
+        // earlier step's Givens stopped the cycle.
+        auto arnoldi_step = [&](int k, const int* skip) -> int {
+            double* W = h->V + (size_t)k * vol;
             {
                 ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN);
-                TRY(launch_ssor_fwd(h, h->V + (size_t)(kit - 1) * vol, nullptr));
+                TRY(launch_ssor_fwd(h, h->V + (size_t)(k - 1) * vol, nullptr, skip));
             }
             {
                 ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
-                TRY(launch_ssor_bwd(h, W));
+                TRY(launch_ssor_bwd(h, W, skip));
             }
-            double* hcol = h->h + (size_t)K1 * (kit - 1);
+            double* hcol = h->h + (size_t)K1 * (k - 1);
             {
-                // passes: <v1,w>; (kit-1) x {w -= h v_k; <v_k+1,w>}; w -= h v_kit, ||w||
-                ProfScope ps(h, TBL_PROF_MGS, (2.0 + 4.0 * (kit - 1) + 3.0) * wN);
-                TRY(launch_mgs(h, W, nullptr, nullptr, V0, &hcol[0], 0));
-                for (int kk = 1; kk <= kit - 1; ++kk)
+                // passes: <v1,w>; (k-1) x {w -= h v_k; <v_k+1,w>}; w -= h v_k, ||w||
+                ProfScope ps(h, TBL_PROF_MGS, (2.0 + 4.0 * (k - 1) + 3.0) * wN);
+                TRY(launch_mgs(h, W, nullptr, nullptr, V0, &hcol[0], 0, skip));
+                for (int kk = 1; kk <= k - 1; ++kk)
                     TRY(launch_mgs(h, W, h->V + (size_t)(kk - 1) * vol, &hcol[kk - 1], h->V + (size_t)kk * vol,
-                                   &hcol[kk], 0));
-                TRY(launch_mgs(h, W, h->V + (size_t)(kit - 1) * vol, &hcol[kit - 1], nullptr, &hcol[kit], 1));
+                                   &hcol[kk], 0, skip));
+                TRY(launch_mgs(h, W, h->V + (size_t)(k - 1) * vol, &hcol[k - 1], nullptr, &hcol[k], 1, skip));
             }
             {
                 ProfScope ps(h, TBL_PROF_SMALL, 0.0);
-                TRY(launch_givens(h, kit));
+                TRY(launch_givens(h, k, skip, h->cfg.errtol));
             }
             {
                 ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
-                TRY(launch_scale_by_inv(h, W, &h->sc->red[8]));
+                TRY(launch_scale_by_inv(h, W, &h->sc->red[8], skip));
             }
-            TRY(readback(h, &h->sc->sumav, sizeof(double)));
-            sumav = h->hpin[0];
+            return TBL_OK;
+        };
+        if (rec || (h->cfg.flags & TBL_FLAG_RB_PRECOND)) {  // one step at a time, read back after each
+            while (rec ? (kit < target) : ((sumav > h->cfg.errtol) && (kit < kmax))) {
+                kit = kit + 1;
+                TRY(arnoldi_step(kit, nullptr));
+                TRY(readback(h, &h->sc->sumav, sizeof(double)));
+                sumav = h->hpin[0];
+            }
+        } else if (sumav > h->cfg.errtol && kmax > 0) {
+            TRY(arnoldi_ahead(h, kmax, h->cfg.errtol, arnoldi_step, kit, sumav));
         }
         iters += kit;
         kits.push_back(kit);

@@ -56,7 +56,8 @@ struct DevScalars {
     double lamda;
     double lamda03;
     int ksep;
-    int pad;
+    int stop;  // set by k_givens when the Arnoldi estimate reaches its target: the kernels
+               // of an Arnoldi step enqueued ahead of the host's check then return at once
     // GMRES
     double rho, sumnor, sumav;
     // reductions (result slots)
@@ -148,6 +149,7 @@ struct tbl_handle {
     int* err;                      // device error word
     // host side
     double* hpin;                  // pinned readback
+    cudaEvent_t ahead_ev[2];       // Arnoldi steps enqueued ahead: the copy of step k's estimate done
     cudaStream_t stream;
     int64_t launches;
     double npts;                   // nx*ny*nz reference points (algorithmic byte counts)

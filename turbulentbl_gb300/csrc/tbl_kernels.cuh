@@ -26,27 +26,28 @@ int build_sweep_ctas(tbl_handle* h);
 int check_cooperative(tbl_handle* h);
 int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity);
 int launch_halo_init(tbl_handle* h, int parity);
-int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8);
-int launch_ssor_bwd(tbl_handle* h, double* out);
-int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8);
-int launch_ssor_bwd_f(tbl_handle* h, float* out);
+int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8, const int* skip = nullptr);
+int launch_ssor_bwd(tbl_handle* h, double* out, const int* skip = nullptr);
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip = nullptr);
+int launch_ssor_bwd_f(tbl_handle* h, float* out, const int* skip = nullptr);
 int selftest_bounded_wait(int* observed, double* seconds);
 
 // tbl_krylov.cu
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);
-int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op);
-int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom);
-int launch_givens(tbl_handle* h, int kit);
+int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op,
+               const int* skip = nullptr);
+int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom, const int* skip = nullptr);
+int launch_givens(tbl_handle* h, int kit, const int* skip = nullptr, double stop_at = 0.0);
 int launch_backsub_update(tbl_handle* h, int kit);
 int launch_restart_init(tbl_handle* h, int first);
 int launch_ppe_resid(tbl_handle* h);
 int red_blocks(tbl_handle* h);
 int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int op);
-int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom);
+int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom, const int* skip = nullptr);
 int launch_backsub_update_f(tbl_handle* h, int kit);
 int launch_restart_init_k(tbl_handle* h, int first, int K1);
-int launch_givens_k(tbl_handle* h, int kit, int K1);
-int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol);
+int launch_givens_k(tbl_handle* h, int kit, int K1, const int* skip = nullptr, double stop_at = 0.0);
+int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol, const int* skip = nullptr);
 
 // tbl_api.cu
 int readback(tbl_handle* h, const void* dev, size_t bytes);

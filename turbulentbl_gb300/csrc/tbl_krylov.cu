@@ -70,7 +70,8 @@ constexpr int MGS_BLOCKS_PER_SM = 4;
 __global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __restrict__ w,
                                                   const double2* __restrict__ vk, const double* __restrict__ hk,
                                                   const double2* __restrict__ vn, RedWork rw, int slot, double* out,
-                                                  int op) {
+                                                  int op, const int* __restrict__ skip) {
+    if (skip && *skip) return;  // an Arnoldi step enqueued ahead of a converged one
     __shared__ double s_red[RED_THREADS / 32];
     const double hv = vk ? *hk : 0.0;
     const unsigned long long keep = l2_keep_policy();
@@ -111,7 +112,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_mgs(long long n2, double2* __re
 }
 
 // w /= *denom when *denom != 0 (:1158-1161); multiplies by the reciprocal
-__global__ void k_scale_inv(long long n2, double2* __restrict__ w, const double* __restrict__ denom) {
+__global__ void k_scale_inv(long long n2, double2* __restrict__ w, const double* __restrict__ denom,
+                            const int* __restrict__ skip) {
+    if (skip && *skip) return;
     const double d = *denom;
     if (!(d > 0.0 || d < 0.0)) return;
     const double r = 1.0 / d;
@@ -132,6 +135,7 @@ __global__ void k_restart_init(int K1, double* h, double* gg, double* gc, double
     __syncthreads();
     if (threadIdx.x == 0) {
         double rho = sc->rho;
+        sc->stop = 0;
         if (first) sc->sumnor = rho;
         sc->sumav = rho / sc->sumnor;
         gg[0] = rho;
@@ -140,8 +144,13 @@ __global__ void k_restart_init(int K1, double* h, double* gg, double* gc, double
 
 // Givens rotations for column kit (1-based) (:1165-1189).  h(kit+1,kit) holds
 // the norm of the orthogonalised vector; it is saved for the normalisation.
-__global__ void k_givens(int K1, int kit, double* h, double* gg, double* gc, double* gs, DevScalars* sc) {
+// With skip (Arnoldi steps enqueued ahead): returns at once when a previous
+// step stopped the cycle, and stops it itself when the estimate sumav reaches
+// stop_at (the host's loop test, evaluated on the same double).
+__global__ void k_givens(int K1, int kit, double* h, double* gg, double* gc, double* gs, DevScalars* sc,
+                         const int* skip, double stop_at) {
     if (threadIdx.x != 0) return;
+    if (skip && *skip) return;
     auto H = [&](int a, int b) -> double& { return h[(a - 1) + K1 * (b - 1)]; };
     sc->red[8] = H(kit + 1, kit);
     if (kit > 1) {
@@ -166,6 +175,7 @@ __global__ void k_givens(int K1, int kit, double* h, double* gg, double* gc, dou
     double rho = fabs(gg[kit]);
     sc->rho = rho;
     sc->sumav = rho / sc->sumnor;
+    if (skip && !(sc->sumav > stop_at)) sc->stop = 1;
 }
 
 // y from the triangular h (:1193-1200), one thread
@@ -248,7 +258,9 @@ __global__ void __launch_bounds__(RED_THREADS, 8) k_dot_f(long long n4, const fl
 }
 
 
-__global__ void k_scale_inv_f(long long n4, float4* __restrict__ w, const double* __restrict__ denom) {
+__global__ void k_scale_inv_f(long long n4, float4* __restrict__ w, const double* __restrict__ denom,
+                              const int* __restrict__ skip) {
+    if (skip && *skip) return;
     const double d = *denom;
     if (!(d > 0.0 || d < 0.0)) return;
     const float r = (float)(1.0 / d);
@@ -286,18 +298,19 @@ int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int
     return TBL_OK;
 }
 
-int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op) {
+int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op,
+               const int* skip) {
     int nb = MGS_BLOCKS_PER_SM * (h->n_sm > 0 ? h->n_sm : 148);
     if (nb > red_blocks(h)) nb = red_blocks(h);
     k_mgs<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, (const double2*)vk, hk, (const double2*)vn,
-                                             h->red, 7, out, op);
+                                             h->red, 7, out, op, skip);
     h->launches++;
     return TBL_OK;
 }
 
-int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom) {
+int launch_scale_by_inv(tbl_handle* h, double* w, const double* denom, const int* skip) {
     int nb = red_blocks(h);
-    k_scale_inv<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, denom);
+    k_scale_inv<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 2, (double2*)w, denom, skip);
     h->launches++;
     return TBL_OK;
 }
@@ -309,9 +322,9 @@ int launch_restart_init(tbl_handle* h, int first) {
     return TBL_OK;
 }
 
-int launch_givens(tbl_handle* h, int kit) {
+int launch_givens(tbl_handle* h, int kit, const int* skip, double stop_at) {
     const int K1 = h->cfg.kmax + 1;
-    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc);
+    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc, skip, stop_at);
     h->launches++;
     return TBL_OK;
 }
@@ -374,8 +387,10 @@ __device__ __forceinline__ double warp_reduce_scatter16(double (&a)[16]) {
 template <int G>
 __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const float4* __restrict__ w,
                                                             const float4* __restrict__ V, long long vstride4, int nv,
-                                                            int g0, double* __restrict__ partial, int max_blocks) {
+                                                            int g0, double* __restrict__ partial, int max_blocks,
+                                                            const int* __restrict__ skip) {
     static_assert(2 * G <= 16, "the warp reduce-scatter takes 16 values");
+    if (skip && *skip) return;
     constexpr int NW = RED_THREADS / 32;
     __shared__ double s_red[16 * NW];
     const int grp = g0 / LSG_G + blockIdx.y;  // slot index of this group
@@ -412,7 +427,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_lsg_dots_f(long long n4, const 
 // partials (lanes strided over the blocks, four loads in flight per lane,
 // then the shuffle tree); d[i] for even slots, g[i] (i < nv-1) for odd.
 __global__ void __launch_bounds__(256) k_lsg_reduce(const double* __restrict__ partial, int max_blocks, int nb,
-                                                    int nv, double* __restrict__ dout, double* __restrict__ gout) {
+                                                    int nv, double* __restrict__ dout, double* __restrict__ gout,
+                                                    const int* __restrict__ skip) {
+    if (skip && *skip) return;
     const int lane = threadIdx.x & 31;
     const int v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // value 0 .. 2 nv - 1
     if (v >= 2 * nv) return;
@@ -441,7 +458,8 @@ __global__ void __launch_bounds__(256) k_lsg_reduce(const double* __restrict__ p
 // when each was the newest.
 __global__ void __launch_bounds__(32) k_lsg_solve(int K1, int nv, double* __restrict__ Lm,
                                                   const double* __restrict__ d, const double* __restrict__ gnew,
-                                                  double* __restrict__ hcol) {
+                                                  double* __restrict__ hcol, const int* __restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ double sL[64][65];
     __shared__ double st[64];
     const int lane = threadIdx.x, r = nv - 1;
@@ -463,7 +481,8 @@ __global__ void __launch_bounds__(32) k_lsg_solve(int K1, int nv, double* __rest
 __global__ void __launch_bounds__(RED_THREADS, 6) k_lsg_update_f(long long n4, float4* __restrict__ w,
                                                               const float4* __restrict__ V, long long vstride4, int nv,
                                                               const double* __restrict__ t, RedWork rw, int slot,
-                                                              double* out) {
+                                                              double* out, const int* __restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ double s_red[RED_THREADS / 32];
     __shared__ float s_t[64];
     for (int i = threadIdx.x; i < nv && i < 64; i += blockDim.x) s_t[i] = (float)t[i];
@@ -487,7 +506,7 @@ __global__ void __launch_bounds__(RED_THREADS, 6) k_lsg_update_f(long long n4, f
     grid_finish(bt, rw, slot, gridDim.x, blockIdx.x, out, 1);
 }
 
-int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
+int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol, const int* skip) {
     const int K1 = h->cfg.mixed_kmax + 1;
     if (kit > 64 || kit > K1) return TBL_ERR_BAD_ARG;
     const int nb = red_blocks(h);
@@ -502,14 +521,14 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
     const float4* Vc = (const float4*)h->Vf;
     if (nfull > 0)
         k_lsg_dots_f<LSG_G><<<dim3(nbd, nfull), RED_THREADS, 0, h->stream>>>(n4, Wc, Vc, n4, kit, 0,
-                                                                             h->lsg_partial, h->red.max_blocks);
+                                                                             h->lsg_partial, h->red.max_blocks, skip);
     if (rem > 0) {
         const int g0 = nfull * LSG_G;
         switch (rem) {
 #define TBL_LSG_REM(R)                                                                                              \
     case R:                                                                                                         \
         k_lsg_dots_f<R><<<dim3(nbd, 1), RED_THREADS, 0, h->stream>>>(n4, Wc, Vc, n4, kit, g0, h->lsg_partial,       \
-                                                                    h->red.max_blocks);                            \
+                                                                    h->red.max_blocks, skip);                      \
         break;
             TBL_LSG_REM(1) TBL_LSG_REM(2) TBL_LSG_REM(3) TBL_LSG_REM(4) TBL_LSG_REM(5) TBL_LSG_REM(6)
             TBL_LSG_REM(7)
@@ -517,12 +536,12 @@ int launch_lsg_f(tbl_handle* h, float* W, int kit, double* hcol) {
         }
     }
     k_lsg_reduce<<<(2 * kit + 7) / 8, 256, 0, h->stream>>>(h->lsg_partial, h->red.max_blocks, nbd, kit, h->lsg_d,
-                                                            h->lsg_g);
-    k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol);  // kit <= 63
+                                                            h->lsg_g, skip);
+    k_lsg_solve<<<1, 32, 0, h->stream>>>(K1, kit, h->lsg_L, h->lsg_d, h->lsg_g, hcol, skip);  // kit <= 63
     int nbu = 6 * (h->n_sm > 0 ? h->n_sm : 148);  // one resident wave at 6 blocks per SM
     if (nbu > nb) nbu = nb;
     k_lsg_update_f<<<nbu, RED_THREADS, 0, h->stream>>>(n4, (float4*)W, (const float4*)h->Vf, n4, kit, hcol, h->red, 7,
-                                                      &hcol[kit]);
+                                                      &hcol[kit], skip);
     h->launches += 3 + (nfull > 0) + (rem > 0);
     return TBL_OK;
 }
@@ -534,9 +553,9 @@ int launch_dot_f(tbl_handle* h, const float* a, const float* b, double* out, int
     return TBL_OK;
 }
 
-int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom) {
+int launch_scale_by_inv_f(tbl_handle* h, float* w, const double* denom, const int* skip) {
     int nb = red_blocks(h);
-    k_scale_inv_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (float4*)w, denom);
+    k_scale_inv_f<<<nb, RED_THREADS, 0, h->stream>>>(h->g.vol / 4, (float4*)w, denom, skip);
     h->launches++;
     return TBL_OK;
 }
@@ -557,8 +576,8 @@ int launch_restart_init_k(tbl_handle* h, int first, int K1) {
     return TBL_OK;
 }
 
-int launch_givens_k(tbl_handle* h, int kit, int K1) {
-    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc);
+int launch_givens_k(tbl_handle* h, int kit, int K1, const int* skip, double stop_at) {
+    k_givens<<<1, 32, 0, h->stream>>>(K1, kit, h->h, h->gg, h->gc, h->gs, h->sc, skip, stop_at);
     h->launches++;
     return TBL_OK;
 }

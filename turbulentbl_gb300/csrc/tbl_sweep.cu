@@ -64,6 +64,7 @@ struct SweepArgs {
     const double* Q8;           // residual mode when non-null
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
     T* OUT;                     // BWD output
+    const int* skip;            // non-null in Arnoldi steps enqueued ahead: return at once when set
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
@@ -170,6 +171,7 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // three velocity components stay co-resident at 512 x 130 x 128.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
+    if (a.skip && *a.skip) return;  // every CTA reads the same word, written by an earlier launch
     constexpr int CH = sweep_ch<Val>();
     constexpr int OPB = 4 * CH;
     constexpr int LG = CH == 8 ? 3 : 2;  // log2(CH)
@@ -639,7 +641,9 @@ template <typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(256) k_lap(Geom g, TC aw, TC as, const TC* __restrict__ Ab,
                                              const TC* __restrict__ At, const TC* __restrict__ Ap,
                                              const TI* __restrict__ X, const double* __restrict__ Q8,
-                                             TO* __restrict__ R, const TO* __restrict__ scale) {
+                                             TO* __restrict__ R, const TO* __restrict__ scale,
+                                             const int* __restrict__ skip) {
+    if (skip && *skip) return;
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > g.nx - 2) return;
@@ -846,15 +850,16 @@ static int launch_gs_sweep_chunk(tbl_handle* h, const int* comps, int ncomp, int
 }
 
 // Forward SSOR sweep of r = L7 X (Q8 == nullptr) or r = Q8 - L7 X.
-int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8) {
+int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8, const int* skip) {
     const Geom& g = h->g;
     k_lap<double, double, double><<<dim3((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2), 256, 0, h->stream>>>(
         g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
-        h->lap_scale);
+        h->lap_scale, skip);
     h->launches++;
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
+    a.skip = skip;
     return launch_sweep<SW_FWD, double>(h, a, a.nib);
 }
 
@@ -870,37 +875,39 @@ static int rb_ssor(tbl_handle* h, T aw, T as, const T* Ab, const T* At, const T*
     return TBL_OK;
 }
 
-int launch_ssor_bwd(tbl_handle* h, double* out) {
+int launch_ssor_bwd(tbl_handle* h, double* out, const int* skip) {
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND)
         return rb_ssor<double>(h, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At,
                                h->lap_scale, h->RH, out);
     SweepArgs<double> a = base_args<double>(h);
     a.RH = h->RH;
     a.OUT = out;
+    a.skip = skip;
     return launch_sweep<SW_BWD, double>(h, a, a.nib);
 }
 
 // Mixed precision: FP32 preconditioned matvec of the inner GMRES.  Xd (FP64
 // outer residual, r = Q8 - L7 p' computed in FP64) or Xf (inner FP32 vector).
-int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8) {
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip) {
     const Geom& g = h->g;
     dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
     const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
     if (PCd)
         k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf,
-                                                                  h->coef_f + 3 * (size_t)g.nz);
+                                                                  h->coef_f + 3 * (size_t)g.nz, skip);
     else
         k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, (float)aw, (float)as, h->coef_f,
                                                                 h->coef_f + g.nz, h->coef_f + 2 * (size_t)g.nz, Xf,
-                                                                nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz);
+                                                                nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz, skip);
     h->launches++;
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
+    a.skip = skip;
     return launch_sweep<SW_FWD, float>(h, a, a.nib);
 }
 
-int launch_ssor_bwd_f(tbl_handle* h, float* out) {
+int launch_ssor_bwd_f(tbl_handle* h, float* out, const int* skip) {
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) {
         const size_t nz = (size_t)h->g.nz;
         return rb_ssor<float>(h, (float)(1.0 / (h->cfg.dx * h->cfg.dx)), (float)(1.0 / (h->cfg.dy * h->cfg.dy)),
@@ -909,6 +916,7 @@ int launch_ssor_bwd_f(tbl_handle* h, float* out) {
     SweepArgs<float> a = base_args<float>(h);
     a.RH = h->RHf;
     a.OUT = out;
+    a.skip = skip;
     return launch_sweep<SW_BWD, float>(h, a, a.nib);
 }
 
