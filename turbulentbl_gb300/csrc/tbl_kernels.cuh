@@ -32,6 +32,11 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
 int launch_ssor_bwd_f(tbl_handle* h, float* out, const int* skip = nullptr);
 int selftest_bounded_wait(int* observed, double* seconds);
 
+// tbl_lap.cu: R = scale(k) L7 X by TMA plane tiles (the Arnoldi matvec)
+template <typename T>
+int launch_lap_tma(tbl_handle* h, const T* X, T* R, T aw, T as, const T* Ab, const T* At, const T* Ap, const T* scale,
+                   const int* skip);
+
 // tbl_krylov.cu
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);
 int launch_mgs(tbl_handle* h, double* w, const double* vk, const double* hk, const double* vn, double* out, int op,

@@ -852,9 +852,9 @@ static int launch_gs_sweep_chunk(tbl_handle* h, const int* comps, int ncomp, int
 // Forward SSOR sweep of r = L7 X (Q8 == nullptr) or r = Q8 - L7 X.
 int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8, const int* skip) {
     const Geom& g = h->g;
+    const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
     k_lap<double, double, double><<<dim3((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2), 256, 0, h->stream>>>(
-        g, 1.0 / (h->cfg.dx * h->cfg.dx), 1.0 / (h->cfg.dy * h->cfg.dy), h->Ab, h->At, h->Ap, X, Q8, h->RH,
-        h->lap_scale, skip);
+        g, aw, as, h->Ab, h->At, h->Ap, X, Q8, h->RH, h->lap_scale, skip);
     h->launches++;
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;  // the red-black passes run in launch_ssor_bwd
     SweepArgs<double> a = base_args<double>(h);
@@ -895,10 +895,12 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
     if (PCd)
         k_lap<double, float, double><<<grid, 256, 0, h->stream>>>(g, aw, as, h->Ab, h->At, h->Ap, PCd, Q8, h->RHf,
                                                                   h->coef_f + 3 * (size_t)g.nz, skip);
-    else
-        k_lap<float, float, float><<<grid, 256, 0, h->stream>>>(g, (float)aw, (float)as, h->coef_f,
-                                                                h->coef_f + g.nz, h->coef_f + 2 * (size_t)g.nz, Xf,
-                                                                nullptr, h->RHf, h->coef_f + 3 * (size_t)g.nz, skip);
+    else {  // the inner Arnoldi matvec: TMA plane tiles
+        const int s = launch_lap_tma<float>(h, Xf, h->RHf, (float)aw, (float)as, h->coef_f, h->coef_f + g.nz,
+                                            h->coef_f + 2 * (size_t)g.nz, h->coef_f + 3 * (size_t)g.nz, skip);
+        if (s != TBL_OK) return s;
+        h->launches--;  // counted by launch_lap_tma
+    }
     h->launches++;
     if (h->cfg.flags & TBL_FLAG_RB_PRECOND) return TBL_OK;
     SweepArgs<float> a = base_args<float>(h);
