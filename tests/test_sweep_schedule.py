@@ -65,7 +65,14 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
         for kg in range(nkg):
             for jb in range(njb):
                 ctas.append(dict(slab=r, jb=jb, kg=kg, up_j=base + kg * njb + (jb - 1) if jb > 0 else -1,
-                                 up_k=base + (kg - 1) * njb + jb if kg > 0 else -1))
+                                 up_k=base + (kg - 1) * njb + jb if kg > 0 else -1,
+                                 dn_j=jb < njb - 1, dn_k=kg < nkg - 1))
+
+    def publishes(cidx, wid):
+        """The kernel's rule for the device-scope progress flag of a warp."""
+        c = ctas[cidx]
+        j_reader = c['dn_j'] and not (mode != 0 and jb_rows > 0 and (32 * (c['jb'] + 1)) % jb_rows == 0)
+        return j_reader or (wid == KG - 1 and c['dn_k'])
     nz = bn + 1
     ps = sx * ny
     vol = ps * nz
@@ -232,6 +239,7 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
             # waits: producers must have completed the target steps (in the snapshot)
             if cta['up_j'] >= 0 and 32 * cta['jb'] != inf['jblk0'] and T - T0 < inf['Cl']:
                 up = (cta['up_j'], by, wid)
+                assert publishes(cta['up_j'], wid), "j producer does not publish its progress"
                 tgt = T - 1
                 assert tgt <= info[up]['T1'], ("j target beyond producer's last step", tgt, info[up]['T1'])
                 assert snap_done[up] >= tgt, ("j producer behind", T, snap_done[up], tgt)
@@ -242,6 +250,7 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
                     up = (cidx, by, wid - 1)
                 else:
                     up = (cta['up_k'], by, KG - 1)
+                    assert publishes(cta['up_k'], KG - 1), "k producer does not publish its progress"
                 assert info[up]['T1'] == tend_k, ("tend_k", info[up]['T1'], tend_k)
                 assert snap_done[up] >= tgt
                 checks['k_wait'] += 1
@@ -467,6 +476,10 @@ def test_model_mirrors_the_kernel_source():
         "const int qlo = max(1, MODE == SW_BWD ? ibase - (g.nx - 2) : 1 - ibase);",
         "const int qhi = min(Q - 1, MODE == SW_BWD ? ibase - 1 : g.nx - 2 - ibase);",
         "const bool full_warp = plag == 1 && 32 * cta.jb + 31 < J;",
+        "const bool j_reader = cta.dn_j && !(MODE != SW_GS && a.jb_rows > 0 && (32 * (cta.jb + 1)) % a.jb_rows == 0);",
+        "const bool publish = j_reader || (wid == KG - 1 && cta.dn_k);",
+        "c.dn_j = jb < njb - 1 ? 1 : 0;",
+        "c.dn_k = kg < nkg - 1 ? 1 : 0;",
         "const bool ok = (full_warp && q0 - 31 >= qlo && q0 + CH - 1 <= qhi) ? step(T, std::true_type{})",
         "a.plag = h->g.ny - 2 <= sweep_ch<T>() ? sweep_ch<T>() : 1;",
         "constexpr int RING = 4;",

@@ -44,6 +44,8 @@ struct SweepCta {
     int jb, kg;    // block coordinates inside the slab
     int up_j;      // CTA index of (jb-1, kg) or -1
     int up_k;      // CTA index of (jb, kg-1) or -1
+    int dn_j;      // 1 when a CTA (jb+1, kg) exists (it reads this CTA's last rows)
+    int dn_k;      // 1 when a CTA (jb, kg+1) exists (its warp 0 reads this CTA's last plane)
 };
 
 // Slab s covers interior planes k in [bn, bn+K) (0-based).

@@ -239,6 +239,12 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
         (cta.up_j >= 0 && 32 * cta.jb != jblk0) ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
     const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
     unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
+    // the device-scope progress flag (a fence of ~1100 cycles every PUB
+    // steps) is published only by warps that another CTA waits for: the
+    // block below in j (unless span blocks restart there) and, for the last
+    // warp, the CTA above in k
+    const bool j_reader = cta.dn_j && !(MODE != SW_GS && a.jb_rows > 0 && (32 * (cta.jb + 1)) % a.jb_rows == 0);
+    const bool publish = j_reader || (wid == KG - 1 && cta.dn_k);
     const unsigned long long tag = a.epoch << 20;
     // physical i of position q
     const int ibase = MODE == SW_BWD ? CH * c_hi + CH - 1 : CH * c_lo;
@@ -456,7 +462,7 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
                 if (MODE == SW_GS && hout) hout[ix[e]] = out[e];
             }
         }
-        if ((T - T0) % PUB == PUB - 1 || T == T1) {
+        if (publish && ((T - T0) % PUB == PUB - 1 || T == T1)) {
             __syncwarp();
             if (lane == 0) st_release(fme, tag + (unsigned long long)(T + 1));
         }
@@ -720,6 +726,8 @@ int build_sweep_ctas(tbl_handle* h) {
                 c.slab = r; c.jb = jb; c.kg = kg;
                 c.up_j = jb > 0 ? base + kg * njb + (jb - 1) : -1;
                 c.up_k = kg > 0 ? base + (kg - 1) * njb + jb : -1;
+                c.dn_j = jb < njb - 1 ? 1 : 0;
+                c.dn_k = kg < nkg - 1 ? 1 : 0;
                 ctas.push_back(c);
             }
     }
