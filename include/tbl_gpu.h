@@ -209,6 +209,11 @@ int tbl_download_state(tbl_handle* h, tbl_state* st);
 
 /* Download the statistics accumulators and rescaling outputs. */
 int tbl_download_stats(tbl_handle* h, tbl_stats_out* out);
+/* The statistics of the last rescaling: the running sums divided by cum
+ * before they are reset (dnstbl2/dnstbl.f90:2021-2049, :2063-2078) -- u, v,
+ * w, uu, vv, ww, uv, uw, vw, nx*nz doubles each (Fortran order), 9*nx*nz in
+ * all; zeros before the first rescaling. */
+int tbl_download_averages(tbl_handle* h, double* avg);
 
 /* Replay iteration counts (parity runs).  rec is a sequence of per-step
  * records {gs1, gs2, gs3, nrestarts, kit_1 .. kit_nrestarts}; used when
@@ -410,6 +415,45 @@ int tbl_statdata_read(const char* path, int32_t nx, int32_t nz, int32_t irec, tb
 #define TBL_INFLOW_RECORDS 37
 int tbl_inflow_profile_read(const char* path, int32_t nz, double* ume1);
 int tbl_inflow_profile_write(const char* path, int32_t nz, const double* x3, const double* ume1);
+
+/* ------------------------------------------------------------ monitor files
+ * Host-only writers of the files the reference's rank 0 writes during a run,
+ * record for record and in its edit descriptors.  Files the reference opens
+ * with ACCESS='APPEND' get the records appended, the others are rewritten.
+ * (nx,nz) arrays in Fortran order.  The values come from tbl_step_stats,
+ * tbl_download_stats, tbl_download_state and tbl_download_averages; the
+ * schedule (every step, every 500 steps, every rescaling, every 100th step
+ * of a rescaling) is the caller's, as in turbulentbl_gb300/monitor.py. */
+/* massflow.xy: time, UbDNS(1..5), 6(1X,F15.7) (dnstbl2/dnstbl.f90:1613-1615) */
+int tbl_monitor_massflow(const char* path, double time, const double* ubulk);
+/* numrcltauwall.xy, per i = 2..nx-1: time, x1, tauw/(ny-2), Cf, 4(1X,F15.7)
+ * (:1670-1681); tauw_window as in tbl_stats_out */
+int tbl_monitor_tauwall(const char* path, double time, int32_t nx, int32_t ny, double ue, const double* x1,
+                        const double* tauw_window);
+/* kineticenergy.dat: time, ke, 2(2X,E20.10) (:1718-1721) */
+int tbl_monitor_kinetic_energy(const char* path, double time, double ke);
+/* lamda.dat: time, lamda, lamda03, 3(2X,F20.10) (:2170-2174) */
+int tbl_monitor_lamda(const char* path, double time, double lamda, double lamda03);
+/* W.dat (rewritten): x1, x3, Wt per (i,k), 3(1X,F15.7) (:2180-2188) */
+int tbl_monitor_blend(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3, const double* wt);
+/* boundarylthickness.dat (rewritten): time, x1, bltkns, deltastar, theta,
+ * Ht, Reth per i, 7(2X,F20.10) (:2258-2267) */
+int tbl_monitor_bl_thickness(const char* path, double time, int32_t nx, const double* x1, const double* bltkns,
+                             const double* deltastar, const double* theta, const double* ht, const double* reth);
+/* k.dat: k, new(k), eta(k) per k, (I5,2(F20.10)) (:2286-2292) */
+int tbl_monitor_knew(const char* path, int32_t nz, const int32_t* newk, const double* eta);
+/* meanvalues.dat: x1, x3, usum2, vsum2, wsum2 per (i,k), 5(1X,F15.7)
+ * (:2296-2302) */
+int tbl_monitor_meanvalues(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3,
+                           const double* usum2, const double* vsum2, const double* wsum2);
+/* Umeanvalues.dat (rewritten): the same and x3*Re, 6(1X,F15.7) (:2098-2104) */
+int tbl_monitor_umeanvalues(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3,
+                            const double* usum2, const double* vsum2, const double* wsum2, double re);
+/* means / medians / taustress (rewritten): one record of a, b, c, 0 per
+ * (i,k), 4(1X,F15.7) each (:2021-2049) -- the u v w, uu vv ww or uv uw vw
+ * blocks of tbl_download_averages */
+int tbl_monitor_averages(const char* path, int32_t nx, int32_t nz, const double* a, const double* b,
+                         const double* c);
 
 #ifdef __cplusplus
 }

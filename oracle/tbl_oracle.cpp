@@ -71,6 +71,7 @@ struct Oracle {
     int nstep = 0, cont = 0, ksep = 0, nstat = 0, cnt2 = 0;
     // statistics
     std::vector<double> usum, vsum, wsum, uusum, vvsum, wwsum, uvsum, uwsum, vwsum;
+    std::vector<double> avg;  // 9 x (nx,nz): the sums / cum of the last rescaling (:2021-2049)
     std::vector<double> deltastar, theta, Ht, Reth, sumxz, tauw_window;
     double ubulk[5] = {0, 0, 0, 0, 0};
     // GMRES work
@@ -181,6 +182,7 @@ int setup(Oracle& o, const tbl_config* cfg, const tbl_mesh* m) {
                     &o.vvsum, &o.wwsum, &o.uvsum, &o.uwsum, &o.vwsum})
         v->assign(n2, 0.0);
     o.ume1.assign(o.nz, 0.0);
+    o.avg.assign((size_t)9 * o.nx * o.nz, 0.0);
     o.newk.assign(o.nz, o.nz - 1);
     for (auto* v : {&o.bltkns, &o.deltastar, &o.theta, &o.Ht, &o.Reth, &o.sumxz, &o.tauw_window}) v->assign(o.nx, 0.0);
     o.V.assign(cfg->kmax + 1, std::vector<double>(o.N, 0.0));
@@ -956,6 +958,13 @@ static void integral_thicknesses(Oracle& o) {
 void rescale(Oracle& o) {
     const int nx = o.nx, ny = o.ny, nz = o.nz, irec = o.c.irec;
     const double cum = (double)o.c.cum, ue = o.c.ue, re = o.c.re;
+    {  // the averaged sums of the means/medians/taustress files (:2028-2048)
+        const std::vector<double>* src[9] = {&o.usum, &o.vsum, &o.wsum, &o.uusum, &o.vvsum, &o.wwsum,
+                                             &o.uvsum, &o.uwsum, &o.vwsum};
+        const size_t n2 = (size_t)nx * nz;
+        for (int m = 0; m < 9; ++m)
+            for (size_t q = 0; q < n2; ++q) o.avg[m * n2 + q] = ((*src[m])[q] / cum);
+    }
     for (int k = 1; k <= nz; ++k)
         for (int i = 1; i <= nx; ++i) {
             size_t q = o.id2(i, k);
@@ -1209,6 +1218,12 @@ int orc_download_stats(orc_handle* h, tbl_stats_out* out) {
     if (out->tauw_window) std::memcpy(out->tauw_window, o.tauw_window.data(), o.nx * 8);
     out->lamda03 = o.lamda03;
     out->nstat = o.nstat;
+    return TBL_OK;
+}
+
+int orc_download_averages(orc_handle* h, double* avg) {
+    if (!h || !avg) return TBL_ERR_BAD_ARG;
+    std::memcpy(avg, h->o.avg.data(), h->o.avg.size() * 8);
     return TBL_OK;
 }
 

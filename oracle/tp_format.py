@@ -1,4 +1,4 @@
-"""Python restatement of the reference's restart and counter files.
+"""Python restatement of the reference's restart, counter and monitor files.
 
 TEST INFRASTRUCTURE ONLY: the checker for the library's C++ readers and
 writers (turbulentbl_gb300/csrc/tbl_restart.cpp, reached through
@@ -21,6 +21,10 @@ Formats (theparvezahmad/turbulentBL):
     (dnssetbl/combineFile.f90:59-61).
   * `cnt` holds "nz cnt proc" (list-directed), `cnt2` holds "cnt2"; dnssetbl's
     statData.dat FORMAT(4(1X,F15.7),I5.3) (dnssetbl.f90:1203-1208).
+  * the monitor files of dnstbl2's rank 0 (massflow.xy, numrcltauwall.xy,
+    kineticenergy.dat, lamda.dat, W.dat, boundarylthickness.dat, k.dat,
+    meanvalues.dat, Umeanvalues.dat, means, medians, taustress;
+    dnstbl2/dnstbl.f90:1613-1721, :2021-2302, formats :2385-2392).
 Format codes: 0 dnstbl2, 1 originalTBL, 2 dnssetbl.
 """
 import os
@@ -278,3 +282,84 @@ def read_inflow_profile(text, nz):
     vals = [fortran_read_e(r.ljust(42)[24:42], 8) for r in recs[:INFLOW_RECORDS]]
     out = np.array([vals[min(k, INFLOW_RECORDS - 1)] for k in range(nz)])
     return out
+
+
+# ------------------------------------------------------------ monitor files
+
+def fortran_f(v, w, d):
+    """Fortran Fw.d: d decimals right-justified in w columns, w asterisks when
+    the value needs more (Python's correctly rounded fixed-point conversion)."""
+    v = float(v)
+    if np.isnan(v):
+        body = "NaN"
+    elif np.isinf(v):
+        body = ("Infinity" if v > 0 else "-Infinity") if w >= 9 else ("Inf" if v > 0 else "-Inf")
+    else:
+        body = f"{v:.{d}f}"
+    return "*" * w if len(body) > w else body.rjust(w)
+
+
+def _f157(*vals):
+    return "".join(" " + fortran_f(v, 15, 7) for v in vals)
+
+
+def _f2010(*vals):
+    return "".join("  " + fortran_f(v, 20, 10) for v in vals)
+
+
+def massflow_text(time, ubulk):
+    """massflow.xy record, FORMAT(6(1X,F15.7)) (dnstbl2/dnstbl.f90:1613-1615)."""
+    return _f157(time, *ubulk[:5]) + "\n"
+
+
+def tauwall_text(time, nx, ny, ue, x1, tauw_window):
+    """numrcltauwall.xy records, i = 2..nx-1, FORMAT(4(1X,F15.7)) (:1674-1679)."""
+    span = float(ny - 2)
+    return "".join(_f157(time, x1[i], tauw_window[i] / span, 2.0 * (tauw_window[i] / (ue * ue * span))) + "\n"
+                   for i in range(1, nx - 1))
+
+
+def kinetic_energy_text(time, ke):
+    """kineticenergy.dat record, FORMAT(2(2X,E20.10)) (:1718-1721)."""
+    return "".join("  " + fortran_e(float(v), 20, 10) for v in (time, ke)) + "\n"
+
+
+def lamda_text(time, lamda, lamda03):
+    """lamda.dat record, FORMAT(3(2X,F20.10)) (:2170-2174)."""
+    return _f2010(time, lamda, lamda03) + "\n"
+
+
+def blend_text(x1, x3, wt):
+    """W.dat, per i, per k: x1, x3, Wt, FORMAT(3(1X,F15.7)) (:2180-2188)."""
+    return "".join(_f157(x1[i], x3[k], wt[i, k]) + "\n" for i in range(len(x1)) for k in range(len(x3)))
+
+
+def bl_thickness_text(time, x1, bltkns, deltastar, theta, ht, reth):
+    """boundarylthickness.dat, FORMAT(7(2X,F20.10)) (:2258-2267)."""
+    return "".join(_f2010(time, x1[i], bltkns[i], deltastar[i], theta[i], ht[i], reth[i]) + "\n"
+                   for i in range(len(x1)))
+
+
+def knew_text(newk, eta):
+    """k.dat records k, new(k), eta(k), FORMAT(I5,2(F20.10)) (:2286-2292)."""
+    return "".join(f"{k + 1:5d}" + fortran_f(float(newk[k]), 20, 10) + fortran_f(eta[k], 20, 10) + "\n"
+                   for k in range(len(newk)))
+
+
+def meanvalues_text(x1, x3, u, v, w, re=None):
+    """meanvalues.dat (FORMAT(5(1X,F15.7)), :2296-2302) or, with re,
+    Umeanvalues.dat (x3*Re appended, FORMAT(6(1X,F15.7)), :2098-2104)."""
+    out = []
+    for i in range(len(x1)):
+        for k in range(len(x3)):
+            c = (x1[i], x3[k], u[i, k], v[i, k], w[i, k]) + (() if re is None else (x3[k] * re,))
+            out.append(_f157(*c) + "\n")
+    return "".join(out)
+
+
+def averages_text(a, b, c):
+    """means / medians / taustress: one record of a, b, c and a zero
+    temperature column per (i,k), i outer, FORMAT(4(1X,F15.7)) each
+    (:2021-2049)."""
+    nx, nz = a.shape
+    return "".join(_f157(a[i, k], b[i, k], c[i, k], 0.0) for i in range(nx) for k in range(nz)) + "\n"

@@ -183,6 +183,9 @@ def declare(lib, prefix, handle_t=C.c_void_p):
     f = getattr(lib, prefix + "download_stats")
     f.argtypes = [H, C.POINTER(TblStatsOut)]
     f.restype = C.c_int
+    f = getattr(lib, prefix + "download_averages")
+    f.argtypes = [H, C.POINTER(C.c_double)]
+    f.restype = C.c_int
     f = getattr(lib, prefix + "set_replay")
     f.argtypes = [H, _ip, C.c_int64]
     f.restype = C.c_int

@@ -118,7 +118,7 @@ static void free_all(tbl_handle* h) {
     void* ptrs[] = {h->U[0], h->U[1], h->U[2], h->Pr, h->PC, h->Q[0], h->Q[1], h->Q[2], h->Q8, h->RH, h->V,
                     h->uold1, h->x3, h->jacinv, h->jac2, h->Ab, h->At, h->Ap, h->rAp, h->gs_coef, h->gs_coef_f, h->lap_scale, h->coef_f, h->usum2, h->vsum2,
                     h->wsum2, h->wt, h->ume1, h->bltkns, h->newk, h->ufl_file, h->ufl_live, h->ufl_full,
-                    h->usum2_fl, h->sums, h->bl_out, h->ubulk, h->sumxz, h->tauw_win, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
+                    h->usum2_fl, h->sums, h->avg, h->bl_out, h->ubulk, h->sumxz, h->tauw_win, h->slab_of_k, h->sc, h->h, h->gg, h->gc, h->gs, h->gy,
                     h->red.partial, h->red.count, h->halo, h->flags, h->ctas, h->slabs, h->err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -222,7 +222,7 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
     TRY(dalloc(&h->ume1, (size_t)nz)); TRY(dalloc(&h->bltkns, (size_t)nx)); TRY(dalloc(&h->newk, (size_t)nz));
     TRY(dalloc(&h->ufl_file, 3 * pl)); TRY(dalloc(&h->ufl_live, 3 * pl));
     TRY(dalloc(&h->ufl_full, 3 * vol)); TRY(dalloc(&h->usum2_fl, 3 * n2));
-    TRY(dalloc(&h->sums, 9 * n2)); TRY(dalloc(&h->bl_out, 4 * (size_t)nx));
+    TRY(dalloc(&h->sums, 9 * n2)); TRY(dalloc(&h->avg, 9 * n2)); TRY(dalloc(&h->bl_out, 4 * (size_t)nx));
     TRY(dalloc(&h->ubulk, 5)); TRY(dalloc(&h->sumxz, (size_t)nx)); TRY(dalloc(&h->tauw_win, (size_t)nx));
     TRY(dalloc(&h->slab_of_k, (size_t)nz));
     TRY(dalloc(&h->sc, 1));
@@ -1007,6 +1007,14 @@ int tbl_download_stats(tbl_handle* h, tbl_stats_out* out) {
     TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     out->lamda03 = sc.lamda03;
     out->nstat = h->nstat;
+    return TBL_OK;
+}
+
+int tbl_download_averages(tbl_handle* h, double* avg) {
+    if (!h || !avg) return TBL_ERR_BAD_ARG;
+    const size_t n2 = (size_t)h->cfg.nx * h->cfg.nz;
+    TBL_CUDA_TRY(cudaMemcpyAsync(avg, h->avg, 9 * n2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    TBL_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return TBL_OK;
 }
 

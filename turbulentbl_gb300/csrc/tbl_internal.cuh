@@ -127,6 +127,7 @@ struct tbl_handle {
     double* usum2_fl;  // 3 x (nx,nz): means used by the last per-step Ufluc update
     // statistics
     double* sums;      // 9 x (nx,nz): usum vsum wsum uusum vvsum wwsum uvsum uwsum vwsum
+    double* avg;       // 9 x (nx,nz): sums / cum of the last rescaling, before the reset
     double* bl_out;    // 4 x nx: deltastar theta Ht Reth
     double* ubulk;     // 5: mass flux through the five planes (last step)
     double* sumxz;     // nx: wall-shear accumulator

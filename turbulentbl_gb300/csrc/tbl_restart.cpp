@@ -1,4 +1,5 @@
-// tbl_restart.cpp -- the reference's restart and counter files (host only).
+// tbl_restart.cpp -- the reference's restart, counter and monitor files
+// (host only).
 //
 // Tecplot ASCII POINT files, one record per grid point, i outermost, then j,
 // then k, an empty record before every i block and every j block, three
@@ -69,6 +70,37 @@ void put_f(std::string& out, double v, int w, int d) {
     out += buf;
 }
 
+// Fortran Fw.d output after nb blanks (the nX edit descriptor before the
+// field): the value with d decimals right-justified in w columns, w asterisks
+// when it needs more, NaN and Infinity spelled out.  C's %.*f rounds the
+// exact binary value to nearest, as gfortran's F editing does, and keeps the
+// minus sign of a negative value that rounds to zero, as gfortran does.
+void put_fw(std::string& out, double v, int nb, int w, int d) {
+    char body[400];
+    if (std::isnan(v))
+        snprintf(body, sizeof body, "NaN");
+    else if (std::isinf(v))
+        snprintf(body, sizeof body, "%s", w >= 9 ? (v > 0 ? "Infinity" : "-Infinity") : (v > 0 ? "Inf" : "-Inf"));
+    else
+        snprintf(body, sizeof body, "%.*f", d, v);
+    out.append((size_t)nb, ' ');
+    const int len = (int)strlen(body);
+    if (len > w) {
+        out.append((size_t)w, '*');
+    } else {
+        out.append((size_t)(w - len), ' ');
+        out += body;
+    }
+}
+
+// Fortran Ew.d output after nb blanks.
+void put_ew(std::string& out, double v, int nb, int w, int d) {
+    std::string f;
+    put_e_wd(f, v, w, d);  // one blank, then the field
+    out.append((size_t)nb, ' ');
+    out.append(f, 1, std::string::npos);
+}
+
 inline size_t id3(int nx, int ny, int i, int j, int k) {  // 0-based
     return (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * (size_t)k);
 }
@@ -133,6 +165,14 @@ void point_cols(int format, const tbl_mesh* m, const tbl_state* st, int nx, int 
 
 bool write_file(const char* path, const std::string& s) {
     FILE* f = fopen(path, "wb");
+    if (!f) return false;
+    const bool ok = fwrite(s.data(), 1, s.size(), f) == s.size();
+    return fclose(f) == 0 && ok;
+}
+
+// The monitor files are opened with ACCESS='APPEND' by the reference.
+bool append_file(const char* path, const std::string& s) {
+    FILE* f = fopen(path, "ab");
     if (!f) return false;
     const bool ok = fwrite(s.data(), 1, s.size(), f) == s.size();
     return fclose(f) == 0 && ok;
@@ -546,6 +586,162 @@ int tbl_inflow_profile_write(const char* path, int32_t nz, const double* x3, con
         out += b.substr(1);
         out += "\n";
     }
+    return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// ------------------------------------------------------------ monitor files
+// The files the reference's rank 0 writes during a run, record for record.
+// Those it opens with ACCESS='APPEND' get the records appended; the others
+// are rewritten.  (nx,nz) arrays are in Fortran order, i fastest.
+
+// massflow.xy: time and the five plane mass fluxes UbDNS, FORMAT(6(1X,F15.7))
+// (dnstbl2/dnstbl.f90:1613-1615, :2390).
+int tbl_monitor_massflow(const char* path, double time, const double* ubulk) {
+    if (!path || !ubulk) return TBL_ERR_BAD_ARG;
+    std::string out;
+    put_fw(out, time, 1, 15, 7);
+    for (int q = 0; q < 5; ++q) put_fw(out, ubulk[q], 1, 15, 7);
+    out += "\n";
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// numrcltauwall.xy after a 500-step wall-shear window: per i = 2..nx-1 the
+// time, x1(i), the span-mean shear sumxz(i)/(ny-2) and Cf =
+// 2 (sumxz(i)/(Ue Ue (ny-2))), FORMAT(4(1X,F15.7)) (:1674-1679, :2392);
+// tauw_window is sumxz already divided by 500 (:1670).
+int tbl_monitor_tauwall(const char* path, double time, int32_t nx, int32_t ny, double ue, const double* x1,
+                        const double* tauw_window) {
+    if (!path || !x1 || !tauw_window || nx < 3 || ny < 3) return TBL_ERR_BAD_ARG;
+    std::string out;
+    const double span = (double)(ny - 2);
+    for (int i = 1; i < nx - 1; ++i) {
+        put_fw(out, time, 1, 15, 7);
+        put_fw(out, x1[i], 1, 15, 7);
+        put_fw(out, tauw_window[i] / span, 1, 15, 7);
+        put_fw(out, 2.0 * (tauw_window[i] / (ue * ue * span)), 1, 15, 7);
+        out += "\n";
+    }
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// kineticenergy.dat: time and the fluctuation energy, FORMAT(2(2X,E20.10))
+// (:1718-1721).
+int tbl_monitor_kinetic_energy(const char* path, double time, double ke) {
+    if (!path) return TBL_ERR_BAD_ARG;
+    std::string out;
+    put_ew(out, time, 2, 20, 10);
+    put_ew(out, ke, 2, 20, 10);
+    out += "\n";
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// lamda.dat after a rescaling: time, lamda, lamda03, FORMAT(3(2X,F20.10))
+// (:2170-2174).
+int tbl_monitor_lamda(const char* path, double time, double lamda, double lamda03) {
+    if (!path) return TBL_ERR_BAD_ARG;
+    std::string out;
+    put_fw(out, time, 2, 20, 10);
+    put_fw(out, lamda, 2, 20, 10);
+    put_fw(out, lamda03, 2, 20, 10);
+    out += "\n";
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// W.dat (rewritten): per i, per k: x1(i), x3(k), Wt(i,k), FORMAT(3(1X,F15.7))
+// (:2180-2188, :2388).
+int tbl_monitor_blend(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3, const double* wt) {
+    if (!path || !x1 || !x3 || !wt || nx < 1 || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k) {
+            put_fw(out, x1[i], 1, 15, 7);
+            put_fw(out, x3[k], 1, 15, 7);
+            put_fw(out, wt[(size_t)i + (size_t)nx * k], 1, 15, 7);
+            out += "\n";
+        }
+    return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// boundarylthickness.dat (rewritten): per i: time, x1, bltkns, deltastar,
+// theta, Ht, Reth, FORMAT(7(2X,F20.10)) (:2258-2267).
+int tbl_monitor_bl_thickness(const char* path, double time, int32_t nx, const double* x1, const double* bltkns,
+                             const double* deltastar, const double* theta, const double* ht, const double* reth) {
+    if (!path || !x1 || !bltkns || !deltastar || !theta || !ht || !reth || nx < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int i = 0; i < nx; ++i) {
+        const double c[7] = {time, x1[i], bltkns[i], deltastar[i], theta[i], ht[i], reth[i]};
+        for (double v : c) put_fw(out, v, 2, 20, 10);
+        out += "\n";
+    }
+    return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// k.dat (every 100th step of a rescaling): per k: k, new(k), eta(k),
+// FORMAT(I5,2(F20.10)) (:2286-2292); new(k) is a REAL array there.
+int tbl_monitor_knew(const char* path, int32_t nz, const int32_t* newk, const double* eta) {
+    if (!path || !newk || !eta || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    char buf[32];
+    for (int k = 0; k < nz; ++k) {
+        snprintf(buf, sizeof buf, "%5d", k + 1);
+        out += strlen(buf) > 5 ? std::string(5, '*') : std::string(buf);
+        put_fw(out, (double)newk[k], 0, 20, 10);
+        put_fw(out, eta[k], 0, 20, 10);
+        out += "\n";
+    }
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// meanvalues.dat (every 100th step of a rescaling): per i, per k: x1(i),
+// x3(k), usum2, vsum2, wsum2, FORMAT(5(1X,F15.7)) (:2296-2302, :2387).
+int tbl_monitor_meanvalues(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3,
+                           const double* usum2, const double* vsum2, const double* wsum2) {
+    if (!path || !x1 || !x3 || !usum2 || !vsum2 || !wsum2 || nx < 1 || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k) {
+            const size_t q = (size_t)i + (size_t)nx * k;
+            const double c[5] = {x1[i], x3[k], usum2[q], vsum2[q], wsum2[q]};
+            for (double v : c) put_fw(out, v, 1, 15, 7);
+            out += "\n";
+        }
+    return append_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// Umeanvalues.dat (rewritten at every rescaling): the same columns and
+// x3(k)*Re, FORMAT(6(1X,F15.7)) (:2098-2104, :2386).
+int tbl_monitor_umeanvalues(const char* path, int32_t nx, int32_t nz, const double* x1, const double* x3,
+                            const double* usum2, const double* vsum2, const double* wsum2, double re) {
+    if (!path || !x1 || !x3 || !usum2 || !vsum2 || !wsum2 || nx < 1 || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k) {
+            const size_t q = (size_t)i + (size_t)nx * k;
+            const double c[6] = {x1[i], x3[k], usum2[q], vsum2[q], wsum2[q], x3[k] * re};
+            for (double v : c) put_fw(out, v, 1, 15, 7);
+            out += "\n";
+        }
+    return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
+}
+
+// means, medians, taustress (rewritten at every rescaling): ONE record of
+// four FORMAT(4(1X,F15.7)) fields per (i,k), i outer -- the averaged sums a,
+// b, c and the temperature's, written as zero (no temperature here) --
+// written with ADVANCE='NO' and closed by an empty list-directed WRITE
+// (:2021-2049, :2385).
+int tbl_monitor_averages(const char* path, int32_t nx, int32_t nz, const double* a, const double* b,
+                         const double* c) {
+    if (!path || !a || !b || !c || nx < 1 || nz < 1) return TBL_ERR_BAD_ARG;
+    std::string out;
+    for (int i = 0; i < nx; ++i)
+        for (int k = 0; k < nz; ++k) {
+            const size_t q = (size_t)i + (size_t)nx * k;
+            put_fw(out, a[q], 1, 15, 7);
+            put_fw(out, b[q], 1, 15, 7);
+            put_fw(out, c[q], 1, 15, 7);
+            put_fw(out, 0.0, 1, 15, 7);
+        }
+    out += "\n";
     return write_file(path, out) ? TBL_OK : TBL_ERR_IO;
 }
 

@@ -690,6 +690,13 @@ __global__ void k_stats(Geom g, double dA, double A, const T* __restrict__ U1, c
     sums[6 * n2 + q] += tuv / A; sums[7 * n2 + q] += tuw / A; sums[8 * n2 + q] += tvw / A;
 }
 
+// The averaged statistics of a rescaling, kept for the monitor files: every
+// running sum divided by cum (:2021-2049, :2063-2078), before the reset.
+__global__ void k_averages(long long n9, double cum, const double* __restrict__ sums, double* __restrict__ avg) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n9) avg[q] = sums[q] / cum;
+}
+
 // ------------------------------- rescaling bookkeeping (:2084-2277), 1 block
 __global__ void k_rescale(Geom g, int irec0, double cum, double ue, double re, const double* __restrict__ x3,
                           double* __restrict__ sums, double* __restrict__ usum2, double* __restrict__ vsum2,
@@ -1142,6 +1149,8 @@ int launch_stats(tbl_handle* h) {
 
 int launch_rescale(tbl_handle* h) {
     const Geom& g = h->g;
+    const long long n9 = 9LL * g.nx * g.nz;
+    k_averages<<<(int)((n9 + 255) / 256), 256, 0, h->stream>>>(n9, (double)h->cfg.cum, h->sums, h->avg);
     k_rescale<<<1, 256, 0, h->stream>>>(g, h->cfg.irec - 1, (double)h->cfg.cum, h->cfg.ue, h->cfg.re, h->x3, h->sums,
                                         h->usum2, h->vsum2, h->wsum2, h->wt, h->bltkns, h->newk, h->bl_out, h->sc);
     int n = (g.ny - 2) * (g.nz - 2);
@@ -1155,7 +1164,7 @@ int launch_rescale(tbl_handle* h) {
     else
         k_rescale_tail<double><<<nb, 256, 0, h->stream>>>(g, h->cfg.irec - 1, h->U[0], h->U[1], h->U[2], h->usum2,
                                                           h->vsum2, h->wsum2, h->ufl_live, h->sums, k_lo, k_hi);
-    h->launches += 2;
+    h->launches += 3;
     return TBL_OK;
 }
 

@@ -130,6 +130,19 @@ class AbiRunner:
         out["nstat"] = o.nstat
         return out
 
+    AVERAGES = ("u", "v", "w", "uu", "vv", "ww", "uv", "uw", "vw")
+
+    def download_averages(self):
+        """The running sums divided by cum at the last rescaling, before the
+        reset: {"u", "v", "w", "uu", ..., "vw"} -> (nx, nz) arrays."""
+        nx, ny, nz = self.n3d
+        a = np.zeros(9 * nx * nz)
+        st = self._fn("download_averages")(self._h, abi.dptr(a))
+        if st != abi.TBL_OK:
+            raise TblError(st, self.prefix + "download_averages")
+        return {name: a[q * nx * nz:(q + 1) * nx * nz].reshape((nx, nz), order="F")
+                for q, name in enumerate(self.AVERAGES)}
+
     # ------------------------------------------------------------------- step
     def step(self, nsteps=1, check=True):
         arr = (abi.TblStepStats * max(nsteps, 1))()
