@@ -26,6 +26,7 @@ import pytest
 CH = 4     # points per lane and step in FP64 (8 in FP32: run(..., ch=8))
 KG = 4     # planes (warps) per CTA
 RING = 4   # plane-to-plane slots
+XR = 8     # slots of the cluster ring (the kernel's XR_SLOTS)
 OPB = 16   # operand buffer elements per lane, 4 CH (position q at q % OPB)
 
 
@@ -33,12 +34,16 @@ def fma(a, b, c):
     return a * b + c
 
 
-def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4):
+def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4, xk=False, xr=XR):
     """One sweep of mode 0 (Gauss-Seidel), 1 (forward SSOR) or 2 (backward
     SSOR) over slabs of K_list planes, J span rows and nx points per line,
     by the kernel's schedule with row lag plag (and block lag changed by
     blag_delta) and sequentially.  Returns (points that differ, last step,
-    counts of the waits checked).  ch: points per lane and step."""
+    counts of the waits checked).  ch: points per lane and step.  xk: the
+    CTAs of a slab column form a cluster and hand the plane below over
+    through a ring of XR slots in the upper CTA's shared memory (st.async
+    into the slot, mbarrier phases), instead of global memory and flags;
+    xr: its slots."""
     CH, OPB = ch, 4 * ch
     rnd = random.Random(seed)
     sx = ((nx + 7) + 7) // 8 * 8
@@ -57,22 +62,28 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
     ctas = []
     slabs = []
     bn = 1
+    # slab columns (same slab and row block, kg = 0..nkc-1) are consecutive
+    # CTAs -- a cluster in the kernel -- with idle CTAs above a short slab
+    nkc = max((K + KG - 1) // KG for K in K_list)
     for r, K in enumerate(K_list):
         slabs.append((bn, K))
         bn += K
         nkg = (K + KG - 1) // KG
         base = len(ctas)
-        for kg in range(nkg):
-            for jb in range(njb):
-                ctas.append(dict(slab=r, jb=jb, kg=kg, up_j=base + kg * njb + (jb - 1) if jb > 0 else -1,
-                                 up_k=base + (kg - 1) * njb + jb if kg > 0 else -1,
-                                 dn_j=jb < njb - 1, dn_k=kg < nkg - 1))
+        for jb in range(njb):
+            for kg in range(nkc):
+                live = kg < nkg
+                ctas.append(dict(slab=r, jb=jb, kg=kg,
+                                 up_j=base + (jb - 1) * nkc + kg if live and jb > 0 else -1,
+                                 up_k=base + jb * nkc + (kg - 1) if live and kg > 0 else -1,
+                                 dn_j=live and jb < njb - 1, dn_k=live and kg < nkg - 1))
+    xk = xk and 2 <= nkc <= 8
 
     def publishes(cidx, wid):
         """The kernel's rule for the device-scope progress flag of a warp."""
         c = ctas[cidx]
         j_reader = c['dn_j'] and not (mode != 0 and jb_rows > 0 and (32 * (c['jb'] + 1)) % jb_rows == 0)
-        return j_reader or (wid == KG - 1 and c['dn_k'])
+        return j_reader or (wid == KG - 1 and c['dn_k'] and not xk)
     nz = bn + 1
     ps = sx * ny
     vol = ps * nz
@@ -171,6 +182,7 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
                 warps.append((ci_, by, wid))
     st = {}
     ring = {}   # (cta, by, wid, slot) -> (step, [lane][e])
+    xring = {}  # cluster hand-off: (consumer cta, by, slot) -> (index pushed, [lane][e])
     maxT = 0
     info = {}
     for (cidx, by, wid) in warps:
@@ -221,10 +233,11 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
         issue(w, info[w]['T0'])
         issue(w, info[w]['T0'] + 1)
 
-    checks = dict(j_wait=0, k_wait=0, fast=0)
+    checks = dict(j_wait=0, k_wait=0, fast=0, x_push=0)
     for T in range(0, maxT + 1):
         snapG, snapRH, snapOUT = list(G), list(RH), list(OUT)
         snap_ring = dict(ring)
+        snap_xring = dict(xring)
         snap_done = {w: st[w]['done'] for w in st}
         for w in info:
             inf = info[w]
@@ -250,7 +263,8 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
                     up = (cidx, by, wid - 1)
                 else:
                     up = (cta['up_k'], by, KG - 1)
-                    assert publishes(cta['up_k'], KG - 1), "k producer does not publish its progress"
+                    assert cta['up_k'] // nkc == cidx // nkc, "k producer outside the slab column"
+                    assert xk or publishes(cta['up_k'], KG - 1), "k producer does not publish its progress"
                 assert info[up]['T1'] == tend_k, ("tend_k", info[up]['T1'], tend_k)
                 assert snap_done[up] >= tgt
                 checks['k_wait'] += 1
@@ -314,6 +328,14 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
                     for e in range(CH):
                         if act[e]:
                             assert ent is not None and ent[0] == T - 1, ("ring", ent and ent[0], T - 1)
+                            pk[e] = ent[1][lane][e]
+                elif xk and cta['up_k'] >= 0:
+                    # ring slot (T - T0) % XR holds the producer's (T - T0)-th push, its step T - 1
+                    xu = T - T0
+                    ent = snap_xring.get((cidx, by, xu % xr))
+                    assert ent is not None and ent[0] == xu, ("cluster ring", ent and ent[0], xu)
+                    for e in range(CH):
+                        if act[e]:
                             pk[e] = ent[1][lane][e]
                 else:
                     for e in range(CH):
@@ -388,6 +410,19 @@ def run(mode, nx, J, K_list, plag, jb_rows=0, nib=1, seed=0, blag_delta=0, ch=4)
             has_down = wid < KG - 1 and kl + 1 < K
             if has_down:
                 ring[(cidx, by, wid, T % RING)] = (T, [list(o) for o in out])
+            if xk and wid == KG - 1 and cta['dn_k']:
+                # push to the CTA above: the consumer released this slot's
+                # previous use (index xu - XR, read at its step T0c + xu - XR)
+                cons = (cidx + 1, by, 0)
+                assert ctas[cidx + 1]['up_k'] == cidx and (cidx + 1) // nkc == cidx // nkc
+                xu = T - T0
+                assert info[cons]['T0'] == T0 + 1 and info[cons]['T1'] == T1 + 1
+                if xu >= xr:
+                    assert snap_done[cons] >= info[cons]['T0'] + xu - xr, "slot overwritten before its release"
+                    # the release is sent only for slots written again
+                    assert (xu - xr) + xr <= info[cons]['T1'] - info[cons]['T0']
+                xring[(cidx + 1, by, xu % xr)] = (xu, [list(o) for o in out])
+                checks['x_push'] += 1
             # stores
             for L in lanes:
                 for e in range(CH):
@@ -477,9 +512,19 @@ def test_model_mirrors_the_kernel_source():
         "const int qhi = min(Q - 1, MODE == SW_BWD ? ibase - 1 : g.nx - 2 - ibase);",
         "const bool full_warp = plag == 1 && 32 * cta.jb + 31 < J;",
         "const bool j_reader = cta.dn_j && !(MODE != SW_GS && a.jb_rows > 0 && (32 * (cta.jb + 1)) % a.jb_rows == 0);",
-        "const bool publish = j_reader || (wid == KG - 1 && cta.dn_k);",
-        "c.dn_j = jb < njb - 1 ? 1 : 0;",
-        "c.dn_k = kg < nkg - 1 ? 1 : 0;",
+        "const bool publish = j_reader || (wid == KG - 1 && cta.dn_k && !xk);",
+        "c.up_j = live && jb > 0 ? base + (jb - 1) * nkc + kg : -1;",
+        "c.up_k = live && kg > 0 ? base + jb * nkc + (kg - 1) : -1;",
+        "c.dn_j = live && jb < njb - 1 ? 1 : 0;",
+        "c.dn_k = live && kg < nkg - 1 ? 1 : 0;",
+        "constexpr int XR_SLOTS = 8;",
+        "const bool xprod = xk && wid == KG - 1 && cta.dn_k;",
+        "const bool xcons = xk && wid == 0 && cta.up_k >= 0;",
+        "const int xu = T - T0;",
+        "if (xcons && !mbar_wait(&s_full[xu % XR], (unsigned)(xu / XR) & 1u)) abort = 1;",
+        "if (lane == 0 && xu + XR <= T1 - T0) {",
+        "if (xu >= XR && !mbar_wait(&s_empty[xu % XR], (unsigned)(xu / XR - 1) & 1u)) abort = 1;",
+        "if (nkc >= 2 && nkc <= 8) {",
         "const bool ok = (full_warp && q0 - 31 >= qlo && q0 + CH - 1 <= qhi) ? step(T, std::true_type{})",
         "a.plag = h->g.ny - 2 <= sweep_ch<T>() ? sweep_ch<T>() : 1;",
         "constexpr int RING = 4;",
@@ -495,6 +540,39 @@ def test_specialised_steps_reproduce_the_sequential_sweep(mode, nib):
     bad, _, checks = run(mode, 83, 64, [5, 4], kernel_plag(64), 0, nib)
     assert bad == 0
     assert checks["fast"] > 0
+
+
+def _cluster_cases():
+    out = []
+    for mode in (0, 1, 2):
+        for nx, J, Ks, nib, ch in [(23, 40, (5, 4), 1, 4), (17, 9, (9,), 1, 4), (12, 33, (2, 6, 5), 1, 4),
+                                   (40, 70, (13, 4), 1, 4), (83, 64, (16, 15), 1, 4), (40, 33, (9, 3), 2, 4),
+                                   (83, 64, (5, 4), 1, 8), (30, 9, (13, 4), 1, 8), (150, 40, (9,), 2, 8)]:
+            if mode == 0 and nib > 1:
+                continue
+            out.append((mode, nx, J, Ks, nib, ch))
+    return out
+
+
+@pytest.mark.parametrize("mode,nx,J,Ks,nib,ch", _cluster_cases())
+def test_cluster_hand_off_reproduces_the_sequential_sweep(mode, nx, J, Ks, nib, ch):
+    """Plane groups of a slab column as one cluster: the plane below reaches
+    warp 0 of the upper CTAs through the XR-slot ring (slot and phase of
+    every push and read, release before reuse), also with idle CTAs above a
+    short slab; same steps, same values."""
+    plag = kernel_plag(J, ch)
+    bad, last, checks = run(mode, nx, J, list(Ks), plag, 0, nib, ch=ch, xk=True)
+    assert bad == 0
+    assert checks["x_push"] > 0
+    assert last == run(mode, nx, J, list(Ks), plag, 0, nib, ch=ch)[1]
+
+
+def test_a_one_slot_cluster_ring_would_be_overwritten_before_its_read():
+    """The consumer runs one step behind its producer, so a single slot is
+    refilled before it is read (the kernel's ring has 8)."""
+    with pytest.raises(AssertionError, match="slot overwritten"):
+        run(1, 23, 40, [5, 4], 1, xk=True, xr=1)
+    assert run(1, 23, 40, [5, 4], 1, xk=True, xr=2)[0] == 0
 
 
 def _cases8():

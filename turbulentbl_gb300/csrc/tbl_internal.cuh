@@ -148,6 +148,8 @@ struct tbl_handle {
     tbl::SweepCta* ctas;           // [n_cta]
     tbl::SlabDesc* slabs;          // [P]
     int n_cta;
+    int sweep_kc;                  // CTAs of a slab column (plane groups): one thread-block cluster
+    int sweep_cluster[3][8];       // per sweep mode and grid.y: 1 cluster launch, 0 cooperative, -1 not yet known
     unsigned long long epoch;
     int* err;                      // device error word
     // host side

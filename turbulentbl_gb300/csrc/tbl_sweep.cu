@@ -18,15 +18,18 @@
 //     instead of the nx/4 + K + (ny-2) of a chunk-per-row lag;
 //   * every warp waits only for the warps producing its inputs: the warp of
 //     the row block above (global progress flag, acquire/release) and the
-//     warp of the plane below (shared-memory progress inside the CTA, a
-//     global flag across CTAs); waits are bounded spins, a timeout sets an
-//     error word and the warp returns;
+//     warp of the plane below (shared-memory progress inside the CTA; across
+//     CTAs, a ring in distributed shared memory when the CTAs of a slab
+//     column form a thread-block cluster, else a global flag); waits are
+//     bounded spins, a timeout sets an error word and the warp returns;
 //   * slabs are independent (block-Jacobi GS halos come from a snapshot of the
 //     previous sweep, SSOR halos are zero), so all slabs and, for GS, all three
-//     velocity components run concurrently in one cooperative launch.
+//     velocity components run concurrently in one launch whose CTAs are all
+//     resident (clusters of a slab column's CTAs, or a cooperative launch).
 //
 // The backward SSOR sweep is the same schedule on mirrored indices.
 #include <cooperative_groups.h>
+#include <algorithm>
 #include <type_traits>
 
 #include "tbl_internal.cuh"
@@ -65,6 +68,8 @@ struct SweepArgs {
     T* RH;                      // FWD input r, overwritten with the (unscaled) forward result; BWD input
     T* OUT;                     // BWD output
     const int* skip;            // non-null in Arnoldi steps enqueued ahead: return at once when set
+    int xk;                     // plane-CTA hand-off through distributed shared memory (CTAs of a slab
+                                // column form one cluster along k), 0 = global flags
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
@@ -103,6 +108,7 @@ __device__ __forceinline__ bool wait_shared(volatile int* p, int target) {
 }
 
 constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memory)
+constexpr int XR_SLOTS = 8;  // slots of the ring a CTA receives its plane-below values in (cluster hand-off)
 // Points per lane per step: 4 in FP64 (one 32-byte sector), 8 in FP32.  An
 // FP64 step is bound by its chain of dependent FP64 FMAs (GB300 issues FP64
 // at 1/64 of the FP32 rate), an FP32 step by its fixed synchronisation cost,
@@ -114,7 +120,8 @@ constexpr int RING = 4;  // plane-to-plane exchange slots per warp (shared memor
 template <typename Val> constexpr int sweep_ch() { return sizeof(Val) == 4 ? 8 : 4; }
 // Dynamic shared memory of a sweep CTA: the plane-to-plane ring and the operand buffers.
 template <typename Val> constexpr size_t sweep_smem() {
-    return sizeof(Val) * KG * (RING * 32 * sweep_ch<Val>() + 32 * 4 * sweep_ch<Val>());
+    return sizeof(Val) * KG * (RING * 32 * sweep_ch<Val>() + 32 * 4 * sweep_ch<Val>()) +
+           sizeof(Val) * XR_SLOTS * 32 * sweep_ch<Val>();
 }
 
 // 16-byte asynchronous global -> shared copy (cp.async, L2 only), its group
@@ -128,6 +135,105 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 constexpr int PUB = 4;   // global progress is published every PUB steps (and at the end)
+
+// ---- plane hand-off across the CTAs of a cluster (distributed shared memory)
+// The CTAs of a slab column (same slab and row block, plane groups
+// kg = 0..nkc-1) form one thread-block cluster.  The last warp of a CTA
+// pushes each step's CH values per lane into a ring of XR slots in the
+// shared memory of the CTA above with st.async, whose bytes complete a
+// transaction on that slot's "full" mbarrier there; the consumer (warp 0 of
+// that CTA) waits for the slot's phase, reads it, re-arms it and frees it
+// with a remote arrive on the producer's "empty" mbarrier.  No fence and no
+// global flag: the mbarrier phases order the data (the pattern of a TMA
+// pipeline: default CTA-scope semantics on the wait and the remote arrive;
+// cluster-scope release on the arrive measured 10-12% slower sweeps, as it
+// waits for the warp's earlier global stores).  Lifetimes: every remote
+// access targets a warp that waits for it (the consumer waits for every
+// step it is sent, the producer for every slot release it is sent), and two
+// end words keep a warp alive while its partner may still reach its shared
+// memory after a timeout: the producer reports its end (1) or abort (2) to
+// the consumer, and after an abort waits for the consumer's acknowledgement.
+constexpr int XR = XR_SLOTS;
+constexpr long long XLINGER = 1LL << 27;  // bounded wait for the partner at the end
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned mapa_rank(unsigned addr, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(unsigned raddr) {
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(raddr) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the completion of the phase of the given parity.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
+    long long spins = 0;
+    while (!mbar_try_wait(b, parity)) {
+        if (++spins > SPIN_LIMIT) return false;
+    }
+    return true;
+}
+// One lane's CH values of a step into the consumer's ring slot.
+template <int CH>
+__device__ __forceinline__ void xpush(unsigned rd, unsigned rb, const double (&v)[CH]) {
+#pragma unroll
+    for (int b = 0; b < CH / 2; ++b)
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(
+                         rd + 16u * b),
+                     "d"(v[2 * b]), "d"(v[2 * b + 1]), "r"(rb)
+                     : "memory");
+}
+template <int CH>
+__device__ __forceinline__ void xpush(unsigned rd, unsigned rb, const float (&v)[CH]) {
+#pragma unroll
+    for (int b = 0; b < CH / 4; ++b)
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                         rd + 16u * b),
+                     "f"(v[4 * b]), "f"(v[4 * b + 1]), "f"(v[4 * b + 2]), "f"(v[4 * b + 3]), "r"(rb)
+                     : "memory");
+}
+__device__ __forceinline__ void st_remote_s32(unsigned raddr, int v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.s32 [%0], %1;" ::"r"(raddr), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_cluster(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.cluster.shared::cta.s32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+// Bounded wait until a word of this CTA (written by the partner CTA) is non-zero.
+__device__ __forceinline__ int wait_word(const int* p) {
+    for (long long spins = 0; spins < XLINGER; ++spins) {
+        const int v = ld_relaxed_cluster(p);
+        if (v) return v;
+        if (spins > 64) __nanosleep(64);
+    }
+    return 0;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 __device__ __forceinline__ int ld_acquire_cta(const int* p) {
     int v;
@@ -151,7 +257,8 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // Every warp is an independent unit of the dataflow: it waits only for the
 // warps that produce its (j-1) and (k-1) inputs and publishes its own
 // progress (shared memory every step for the next plane in the CTA, a global
-// flag every PUB steps for the CTAs downstream).  No CTA-wide barrier.
+// flag every PUB steps for the CTAs downstream, or, in a cluster, each step's
+// values pushed into the next CTA's ring).  No CTA-wide barrier.
 //
 // Per step a lane updates CH points of its line.  The point update is
 // reassociated so that only one FMA depends on the previous point:
@@ -164,10 +271,12 @@ __device__ __forceinline__ bool wait_cta(const int* p, int target) {
 // Operands of step T that do not depend on other lines arrive in shared
 // memory two steps ahead (cp.async) and are read before the warp waits for
 // its producers; the (k-1) values of the plane below come through a shared
-// memory ring (RING steps deep, with back-pressure), the (j-1) values of the
-// row above by shuffle within the step or, for lane 0, from global memory.
-// Both precisions keep 4 CTAs per SM (at most 128 registers; 64 KB of shared
-// memory in FP64 and 32 KB in FP32), so that the Gauss-Seidel sweeps of the
+// memory ring (RING steps deep, with back-pressure; XR steps deep and filled
+// by st.async from the CTA below for warp 0 of a cluster's upper CTAs), the
+// (j-1) values of the row above by shuffle within the step or, for lane 0,
+// from global memory.
+// Both precisions keep 4 CTAs per SM (at most 128 registers; 40 KB of shared
+// memory in FP64 and 24 KB in FP32), so that the Gauss-Seidel sweeps of the
 // three velocity components stay co-resident at 512 x 130 x 128.
 template <int MODE, typename Val>
 __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
@@ -197,8 +306,29 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     Val (*s_ring)[RING][32][CH] = reinterpret_cast<Val (*)[RING][32][CH]>(s_dyn);
     Val (*s_op)[32][OPB] = reinterpret_cast<Val (*)[32][OPB]>(s_dyn + sizeof(Val) * KG * RING * 32 * CH);
+    Val (*s_xring)[32][CH] =
+        reinterpret_cast<Val (*)[32][CH]>(s_dyn + sizeof(Val) * KG * (RING * 32 * CH + 32 * OPB));
+    __shared__ __align__(8) unsigned long long s_full[XR], s_empty[XR];
+    __shared__ int s_xend, s_xack;  // written by the partner CTA: producer finished (1) / aborted (2); abort seen
+    constexpr unsigned XBYTES = 32 * CH * sizeof(Val);  // one step of a warp
     if (lane == 0) s_prog[wid] = -1;
+    const bool xk = a.xk > 1;
+    if (xk && threadIdx.x == 0) {
+        for (int q = 0; q < XR; ++q) {
+            mbar_init(&s_full[q], 1);
+            mbar_init(&s_empty[q], 1);
+        }
+        s_xend = 0;
+        s_xack = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
+    // the consumer arms every slot for its first phase before any producer
+    // can write (a transaction may also complete before it is armed)
+    if (xk && threadIdx.x == 0 && cta.up_k >= 0)
+        for (int q = 0; q < XR; ++q) mbar_arrive_expect_tx(&s_full[q], XBYTES);
+    if (xk) cluster_sync_all();  // barriers initialised in every CTA of the cluster
+    const unsigned xrank = xk ? cluster_rank() : 0u;
 
     const int jl = 32 * cta.jb + lane;  // logical row
     // SSOR with span blocks: rows restart the schedule at every block of
@@ -237,14 +367,17 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
     const bool has_down = wid < KG - 1 && kl + 1 < K;
     const unsigned long long* fj =
         (cta.up_j >= 0 && 32 * cta.jb != jblk0) ? &flags[(size_t)cta.up_j * KG + wid] : nullptr;
-    const unsigned long long* fk = (wid == 0 && cta.up_k >= 0) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
+    const unsigned long long* fk =
+        (wid == 0 && cta.up_k >= 0 && !xk) ? &flags[(size_t)cta.up_k * KG + KG - 1] : nullptr;
+    const bool xprod = xk && wid == KG - 1 && cta.dn_k;  // pushes its plane to the CTA above in the cluster
+    const bool xcons = xk && wid == 0 && cta.up_k >= 0;   // receives the plane below from the CTA below
     unsigned long long* fme = &flags[(size_t)blockIdx.x * KG + wid];
     // the device-scope progress flag (a fence of ~1100 cycles every PUB
     // steps) is published only by warps that another CTA waits for: the
     // block below in j (unless span blocks restart there) and, for the last
     // warp, the CTA above in k
     const bool j_reader = cta.dn_j && !(MODE != SW_GS && a.jb_rows > 0 && (32 * (cta.jb + 1)) % a.jb_rows == 0);
-    const bool publish = j_reader || (wid == KG - 1 && cta.dn_k);
+    const bool publish = j_reader || (wid == KG - 1 && cta.dn_k && !xk);
     const unsigned long long tag = a.epoch << 20;
     // physical i of position q
     const int ibase = MODE == SW_BWD ? CH * c_hi + CH - 1 : CH * c_lo;
@@ -386,7 +519,11 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
                 }
             }
         }
-        if (__shfl_sync(0xffffffffu, abort, 0)) return false;
+        // the plane below from the CTA below in the cluster: its step T-1 is
+        // the (T - T0)-th it pushes, in ring slot (T - T0) % XR
+        const int xu = T - T0;
+        if (xcons && !mbar_wait(&s_full[xu % XR], (unsigned)(xu / XR) & 1u)) abort = 1;
+        if (__any_sync(0xffffffffu, abort)) return false;
         // ---- inputs of the plane below (same positions, one step earlier)
         // and of the row above for lane 0 (chunk-aligned: lane 0 lags by 0)
         Val pk[CH], pj0[CH];
@@ -397,11 +534,20 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
         } else {
 #pragma unroll
             for (int e = 0; e < CH; ++e)
-                pk[e] = !act[e] ? Val(0) : (pk_ok ? pk_pf[e] : (kin_zero ? Val(0) : __ldcg(kin + ix[e])));
+                pk[e] = !act[e] ? Val(0)
+                                : (xcons ? s_xring[xu % XR][lane][e]
+                                         : (pk_ok ? pk_pf[e] : (kin_zero ? Val(0) : __ldcg(kin + ix[e]))));
         }
 #pragma unroll
         for (int e = 0; e < CH; ++e)
             pj0[e] = (lane != 0 || !act[e]) ? Val(0) : (pj_ok ? pj_pf[e] : (jin_zero ? Val(0) : __ldcg(jin + ix[e])));
+        if (xcons) {  // slot read by every lane: re-arm it and hand it back when it is written again
+            __syncwarp();
+            if (lane == 0 && xu + XR <= T1 - T0) {
+                mbar_arrive_expect_tx(&s_full[xu % XR], XBYTES);
+                if (ld_relaxed_cluster(&s_xend) != 2) mbar_arrive_remote(mapa_rank(smem_u32(&s_empty[xu % XR]), xrank - 1));
+            }
+        }
         if (wrap) {
 #pragma unroll
             for (int e = 0; e < CH; ++e)
@@ -447,6 +593,12 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
             Val* ws = &s_ring[wid][T & (RING - 1)][lane][0];
 #pragma unroll
             for (int e = 0; e < CH; ++e) ws[e] = out[e];
+        }
+        if (xprod) {  // push to the CTA above: wait until the consumer has released the slot's last use
+            if (xu >= XR && !mbar_wait(&s_empty[xu % XR], (unsigned)(xu / XR - 1) & 1u)) abort = 1;
+            if (__any_sync(0xffffffffu, abort)) return false;
+            xpush<CH>(mapa_rank(smem_u32(&s_xring[xu % XR][lane][0]), xrank + 1),
+                      mapa_rank(smem_u32(&s_full[xu % XR]), xrank + 1), out);
         }
         __syncwarp();
         if (lane == 0) st_release_cta(&s_prog[wid], T);
@@ -501,10 +653,24 @@ __global__ void __launch_bounds__(KG * 32, 4) k_sweep(SweepArgs<Val> a) {
         if (!ok) {
             if (lane == 0) atomicExch(a.err, TBL_ERR_TIMEOUT);
             cp_async_wait<0>();  // no copy into this CTA's shared memory outlives the warp
+            if (lane == 0) {
+                // stay until the partner can no longer reach this CTA's shared memory
+                if (xprod) {
+                    st_remote_s32(mapa_rank(smem_u32(&s_xend), xrank + 1), 2);
+                    wait_word(&s_xack);
+                }
+                if (xcons && wait_word(&s_xend) == 2) st_remote_s32(mapa_rank(smem_u32(&s_xack), xrank - 1), 1);
+            }
+            __syncwarp();
             return;
         }
     }
     cp_async_wait<0>();
+    if (lane == 0) {
+        if (xprod) st_remote_s32(mapa_rank(smem_u32(&s_xend), xrank + 1), 1);
+        if (xcons && wait_word(&s_xend) == 2) st_remote_s32(mapa_rank(smem_u32(&s_xack), xrank - 1), 1);
+    }
+    __syncwarp();
 }
 
 // The part of a Gauss-Seidel point update that reads only values the sweep
@@ -715,22 +881,31 @@ int build_sweep_ctas(tbl_handle* h) {
     const int njb = (J + 31) / 32;
     std::vector<SweepCta> ctas;
     std::vector<SlabDesc> slabs(h->P);
+    // The CTAs of a slab column (same slab and row block, kg = 0..nkc-1) are
+    // consecutive, so that they can form one thread-block cluster; slabs
+    // with fewer plane groups get idle CTAs at the top of their columns.
+    int nkc = 1;
+    for (int r = 0; r < h->P; ++r) nkc = std::max(nkc, (h->en[r] - h->bn[r] + 1 + KG - 1) / KG);
     for (int r = 0; r < h->P; ++r) {
         slabs[r].bn = h->bn[r];
         slabs[r].K = h->en[r] - h->bn[r] + 1;
         const int nkg = (slabs[r].K + KG - 1) / KG;
         const int base = (int)ctas.size();
-        for (int kg = 0; kg < nkg; ++kg)
-            for (int jb = 0; jb < njb; ++jb) {
+        for (int jb = 0; jb < njb; ++jb)
+            for (int kg = 0; kg < nkc; ++kg) {
                 SweepCta c;
                 c.slab = r; c.jb = jb; c.kg = kg;
-                c.up_j = jb > 0 ? base + kg * njb + (jb - 1) : -1;
-                c.up_k = kg > 0 ? base + (kg - 1) * njb + jb : -1;
-                c.dn_j = jb < njb - 1 ? 1 : 0;
-                c.dn_k = kg < nkg - 1 ? 1 : 0;
+                const bool live = kg < nkg;
+                c.up_j = live && jb > 0 ? base + (jb - 1) * nkc + kg : -1;
+                c.up_k = live && kg > 0 ? base + jb * nkc + (kg - 1) : -1;
+                c.dn_j = live && jb < njb - 1 ? 1 : 0;
+                c.dn_k = live && kg < nkg - 1 ? 1 : 0;
                 ctas.push_back(c);
             }
     }
+    h->sweep_kc = nkc;
+    for (auto& row : h->sweep_cluster)
+        for (int& v : row) v = -1;
     h->n_cta = (int)ctas.size();
     TBL_CUDA_TRY(cudaMalloc(&h->ctas, ctas.size() * sizeof(SweepCta)));
     TBL_CUDA_TRY(cudaMemcpy(h->ctas, ctas.data(), ctas.size() * sizeof(SweepCta), cudaMemcpyHostToDevice));
@@ -778,7 +953,40 @@ static int launch_sweep(tbl_handle* h, SweepArgs<T>& a, int ncomp) {
     dim3 grid(h->n_cta, ncomp), block(KG * 32);
     // (the dynamic shared memory limit of the three sweep kernels of the
     // handle's precision is raised once, in check_cooperative)
-    TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE, T>, grid, block, args, sweep_smem<T>(), h->stream));
+    // The CTAs of a slab column form one thread-block cluster when they are
+    // 2..8 and the launch's clusters can all be resident at once; the plane
+    // hand-off between them then goes through distributed shared memory.
+    const int nkc = h->sweep_kc;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = sweep_smem<T>();
+    cfg.stream = h->stream;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)nkc;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int& use = h->sweep_cluster[MODE][ncomp < 8 ? ncomp : 7];
+    if (use < 0) {
+        use = 0;
+        int ncl = 0;
+        if (nkc >= 2 && nkc <= 8) {
+            if (cudaOccupancyMaxActiveClusters(&ncl, (const void*)k_sweep<MODE, T>, &cfg) == cudaSuccess)
+                use = (long long)ncl * nkc >= (long long)h->n_cta * ncomp ? 1 : 0;
+            else
+                (void)cudaGetLastError();  // a refused query leaves the cooperative launch
+        }
+    }
+    if (use) {
+        a.xk = nkc;
+        TBL_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_sweep<MODE, T>, a));
+    } else {
+        a.xk = 0;
+        TBL_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_sweep<MODE, T>, grid, block, args, sweep_smem<T>(), h->stream));
+    }
     h->launches++;
     return TBL_OK;
 }
