@@ -199,7 +199,8 @@ static int create_impl(const tbl_config* cfg, const tbl_mesh* mesh, tbl_handle* 
         TRY(dalloc(&h->Pf, vol));
         TRY(dalloc(&h->RHf, vol));
         TRY(dalloc(&h->PREf, 3 * vol));
-        TRY(dalloc(&h->Vf, vol * (size_t)(cfg->mixed_kmax + 1)));
+        // the basis v_0 .. v_kmax, then the Arnoldi vector w before its normalisation
+        TRY(dalloc(&h->Vf, vol * (size_t)(cfg->mixed_kmax + 2)));
         const int K1m = cfg->mixed_kmax + 1, ngr = (K1m + 7) / 8;
         TRY(dalloc(&h->lsg_partial, (size_t)2 * 8 * ngr * 2048));
         TRY(dalloc(&h->lsg_L, (size_t)K1m * K1m));
@@ -472,11 +473,17 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
         // the cycle stops when the estimate reaches the pass's target or its
         // inner tolerance relative to the cycle's start (sumav <= thr)
         const double thr = std::fmax(target, inner_tol * rho_m / sumnor);
+        // w_k is formed in the slot after the basis; step k+1's matvec divides
+        // it by H(k+1,k) as it reads it and writes v_k into the basis (the
+        // separate scaling pass folded into the TMA matvec, same values)
+        float* W = h->Vf + (size_t)K1 * vol;
         auto arnoldi_step = [&](int k, const int* skip) -> int {
-            float* W = h->Vf + (size_t)k * vol;
             {
-                ProfScope ps(h, TBL_PROF_SSOR_FWD, 2.0 * wN);
-                TRY(launch_ssor_fwd_f(h, h->Vf + (size_t)(k - 1) * vol, nullptr, nullptr, skip));
+                ProfScope ps(h, TBL_PROF_SSOR_FWD, (k > 1 ? 3.0 : 2.0) * wN);
+                if (k == 1)
+                    TRY(launch_ssor_fwd_f(h, V0, nullptr, nullptr, skip));
+                else
+                    TRY(launch_ssor_fwd_f(h, W, nullptr, nullptr, skip, &h->sc->red[8], h->Vf + (size_t)(k - 1) * vol));
             }
             {
                 ProfScope ps(h, TBL_PROF_SSOR_BWD, 2.0 * wN);
@@ -492,10 +499,6 @@ static int gmres_mixed(tbl_handle* h, std::vector<int32_t>& kits, tbl_step_stats
             {
                 ProfScope ps(h, TBL_PROF_SMALL, 0.0);
                 TRY(launch_givens_k(h, k, K1, skip, thr));
-            }
-            {
-                ProfScope ps(h, TBL_PROF_VEC, 2.0 * wN);
-                TRY(launch_scale_by_inv_f(h, W, &h->sc->red[8], skip));
             }
             return TBL_OK;
         };

@@ -28,14 +28,15 @@ int launch_gs_sweep(tbl_handle* h, const int* comps, int ncomp, int parity);
 int launch_halo_init(tbl_handle* h, int parity);
 int launch_ssor_fwd(tbl_handle* h, const double* X, const double* Q8, const int* skip = nullptr);
 int launch_ssor_bwd(tbl_handle* h, double* out, const int* skip = nullptr);
-int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip = nullptr);
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip = nullptr,
+                      const double* denom = nullptr, float* vout = nullptr);
 int launch_ssor_bwd_f(tbl_handle* h, float* out, const int* skip = nullptr);
 int selftest_bounded_wait(int* observed, double* seconds);
 
 // tbl_lap.cu: R = scale(k) L7 X by TMA plane tiles (the Arnoldi matvec)
 template <typename T>
 int launch_lap_tma(tbl_handle* h, const T* X, T* R, T aw, T as, const T* Ab, const T* At, const T* Ap, const T* scale,
-                   const int* skip);
+                   const int* skip, const double* denom = nullptr, T* vout = nullptr);
 
 // tbl_krylov.cu
 int launch_dot(tbl_handle* h, const double* a, const double* b, double* out, int op);

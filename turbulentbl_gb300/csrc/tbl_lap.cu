@@ -17,6 +17,12 @@
 // the same time as k_lap's one thread per point; the march is latency-bound
 // (16-row tiles with an eight-stage ring at 2 CTAs per SM took 37 us).
 //
+// In the mixed solver's Arnoldi loop the kernel also finishes the previous
+// step: its input is that step's vector before the division by H(k+1,k),
+// which the kernel applies to each plane tile as it lands, writing the
+// normalised basis vector as it goes (one pass and one launch fewer per
+// Arnoldi step than a separate scaling pass; results bit-identical).
+//
 // Waits are bounded: thread 0 polls the stage's mbarrier at most LT_SPIN
 // times, then sets TBL_ERR_TIMEOUT in the error word, waits (bounded again)
 // for the CTA's other loads in flight and the CTA returns.
@@ -83,7 +89,8 @@ __global__ void __launch_bounds__(LT_THREADS) k_lap_tma(const __grid_constant__ 
                                                         T as, const T* __restrict__ Ab, const T* __restrict__ At,
                                                         const T* __restrict__ Ap, const T* __restrict__ scale,
                                                         T* __restrict__ R, int kc, const int* __restrict__ skip,
-                                                        int* err) {
+                                                        int* err, const double* __restrict__ denom,
+                                                        T* __restrict__ vout) {
     if (skip && *skip) return;  // an Arnoldi step enqueued ahead of a converged one
     constexpr int BX = lt_bx<T>(), RB = lt_row_bytes<T>(), MB = lt_main_bytes<T>(), SB = lt_stage_bytes<T>();
     extern __shared__ __align__(128) unsigned char lt_smem[];
@@ -115,6 +122,29 @@ __global__ void __launch_bounds__(LT_THREADS) k_lap_tma(const __grid_constant__ 
         lt_load(b + RB + MB, &map_row, ib, jp, kk, &full[s]);
     };
     auto parity = [&](int kk) { return (unsigned)(((kk - (k_lo - 1)) / LT_NS) & 1); };
+    // Normalisation folded in (denom non-null): the input is the Arnoldi
+    // vector before its division by H(k+1,k) = *denom; every value of a
+    // stage is multiplied by the same reciprocal the separate pass used,
+    // (T)(1 / d) (none when d is 0), before the stencil reads it, and the
+    // tile's own points of the result go to vout, the basis slot.
+    T rs = T(1);
+    if (denom) {
+        const double d = *denom;
+        if (d > 0.0 || d < 0.0) rs = (T)(1.0 / d);
+    }
+    auto scale_stage = [&](int s) {  // all threads: the three pieces of a stage
+        unsigned char* b = stage(s);
+        T* r0 = reinterpret_cast<T*>(b);
+        T* rm = reinterpret_cast<T*>(b + RB);
+        T* r1 = reinterpret_cast<T*>(b + RB + MB);
+        for (int e = tid; e < BX; e += LT_THREADS) {
+            r0[e] = r0[e] * rs;
+            r1[e] = r1[e] * rs;
+        }
+        for (int e = tid; e < BX * LT_J; e += LT_THREADS) rm[e] = rm[e] * rs;
+        // the stage is refilled by TMA later: order these generic writes before it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    };
     if (tid == 0) {
         for (int s = 0; s < LT_NS; ++s) lt_mb_init(&full[s]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -139,6 +169,14 @@ __global__ void __launch_bounds__(LT_THREADS) k_lap_tma(const __grid_constant__ 
         __syncthreads();
         if (s_abort) break;
         const int sp = (k - 1) & (LT_NS - 1), sc = k & (LT_NS - 1), sn = (k + 1) & (LT_NS - 1);
+        if (denom) {  // planes k-1 and k were scaled as the next plane of earlier iterations
+            if (k == k_lo) {
+                scale_stage(sp);
+                scale_stage(sc);
+            }
+            scale_stage(sn);
+            __syncthreads();
+        }
         const T ab = Ab[k], at = At[k], ap = Ap[k], sk = scale ? scale[k] : T(1);
         for (int r = 1 + tid / LT_I; r <= nr; r += LT_THREADS / LT_I) {
             if (!i_ok) continue;
@@ -151,6 +189,7 @@ __global__ void __launch_bounds__(LT_THREADS) k_lap_tma(const __grid_constant__ 
                           at * row(sn, r)[il + 1] + ap * c[il + 1];
             const long long p = (long long)i + (long long)g.sx * ((long long)(j0 + r - 1) + (long long)g.ny * k);
             R[p] = scale ? sk * lap : lap;
+            if (denom) vout[p] = c[il + 1];
         }
         __syncthreads();  // stage sp is no longer read
         if (tid == 0 && k + LT_NS - 1 <= k_hi + 1) {  // into the stage plane k-1 used
@@ -210,7 +249,8 @@ bool encode(CUtensorMap* m, const T* X, const Geom& g, int rows) {
 // be made.
 template <typename T>
 int launch_lap_tma(tbl_handle* h, const T* X, T* R, T aw, T as, const T* Ab, const T* At, const T* Ap,
-                   const T* scale, const int* skip) {
+                   const T* scale, const int* skip, const double* denom, T* vout) {
+    if ((denom == nullptr) != (vout == nullptr) || (vout && (const T*)vout == X)) return TBL_ERR_BAD_ARG;
     const Geom& g = h->g;
     CUtensorMap rows, row;
     if (!encode<T>(&rows, X, g, LT_J) || !encode<T>(&row, X, g, 1)) {
@@ -237,13 +277,13 @@ int launch_lap_tma(tbl_handle* h, const T* X, T* R, T aw, T as, const T* Ab, con
     const int kc = (planes + nkc - 1) / nkc;
     nkc = (planes + kc - 1) / kc;
     k_lap_tma<T><<<dim3(gx, gy, nkc), LT_THREADS, smem, h->stream>>>(rows, row, g, aw, as, Ab, At, Ap, scale, R, kc,
-                                                                     skip, h->err);
+                                                                     skip, h->err, denom, vout);
     TBL_CUDA_TRY(cudaGetLastError());
     h->launches++;
     return TBL_OK;
 }
 
 template int launch_lap_tma<float>(tbl_handle*, const float*, float*, float, float, const float*, const float*,
-                                   const float*, const float*, const int*);
+                                   const float*, const float*, const int*, const double*, float*);
 
 }  // namespace tbl

@@ -1103,8 +1103,11 @@ int launch_ssor_bwd(tbl_handle* h, double* out, const int* skip) {
 }
 
 // Mixed precision: FP32 preconditioned matvec of the inner GMRES.  Xd (FP64
-// outer residual, r = Q8 - L7 p' computed in FP64) or Xf (inner FP32 vector).
-int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip) {
+// outer residual, r = Q8 - L7 p' computed in FP64) or Xf (inner FP32 vector;
+// with denom, the previous Arnoldi vector before its division by *denom,
+// which the matvec applies, writing the normalised vector to vout).
+int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const double* Q8, const int* skip,
+                      const double* denom, float* vout) {
     const Geom& g = h->g;
     dim3 grid((g.nx - 2 + 255) / 256, g.ny - 2, g.nz - 2);
     const double aw = 1.0 / (h->cfg.dx * h->cfg.dx), as = 1.0 / (h->cfg.dy * h->cfg.dy);
@@ -1113,7 +1116,8 @@ int launch_ssor_fwd_f(tbl_handle* h, const float* Xf, const double* PCd, const d
                                                                   h->coef_f + 3 * (size_t)g.nz, skip);
     else {  // the inner Arnoldi matvec: TMA plane tiles
         const int s = launch_lap_tma<float>(h, Xf, h->RHf, (float)aw, (float)as, h->coef_f, h->coef_f + g.nz,
-                                            h->coef_f + 2 * (size_t)g.nz, h->coef_f + 3 * (size_t)g.nz, skip);
+                                            h->coef_f + 2 * (size_t)g.nz, h->coef_f + 3 * (size_t)g.nz, skip, denom,
+                                            vout);
         if (s != TBL_OK) return s;
         h->launches--;  // counted by launch_lap_tma
     }
