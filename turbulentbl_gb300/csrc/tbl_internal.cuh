@@ -149,7 +149,7 @@ struct tbl_handle {
     tbl::SlabDesc* slabs;          // [P]
     int n_cta;
     int sweep_kc;                  // CTAs of a slab column (plane groups): one thread-block cluster
-    int sweep_cluster[3][8];       // per sweep mode and grid.y: 1 cluster launch, 0 cooperative, -1 not yet known
+    int sweep_cluster[2][3][8];    // per precision, sweep mode and grid.y: 1 cluster launch, 0 cooperative, -1 unknown
     unsigned long long epoch;
     int* err;                      // device error word
     // host side

@@ -904,8 +904,9 @@ int build_sweep_ctas(tbl_handle* h) {
             }
     }
     h->sweep_kc = nkc;
-    for (auto& row : h->sweep_cluster)
-        for (int& v : row) v = -1;
+    for (auto& prec : h->sweep_cluster)
+        for (auto& row : prec)
+            for (int& v : row) v = -1;
     h->n_cta = (int)ctas.size();
     TBL_CUDA_TRY(cudaMalloc(&h->ctas, ctas.size() * sizeof(SweepCta)));
     TBL_CUDA_TRY(cudaMemcpy(h->ctas, ctas.data(), ctas.size() * sizeof(SweepCta), cudaMemcpyHostToDevice));
@@ -969,7 +970,7 @@ static int launch_sweep(tbl_handle* h, SweepArgs<T>& a, int ncomp) {
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    int& use = h->sweep_cluster[MODE][ncomp < 8 ? ncomp : 7];
+    int& use = h->sweep_cluster[sizeof(T) == 8 ? 1 : 0][MODE][ncomp < 8 ? ncomp : 7];
     if (use < 0) {
         use = 0;
         int ncl = 0;
