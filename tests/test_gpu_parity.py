@@ -39,12 +39,17 @@ def compare(o, g, fields=("u", "v", "w", "p", "pcorr")):
 
 
 @pytest.mark.parametrize("nx,nzs,nyw,P", [(24, 12, 20, 2), (30, 10, 26, 3), (21, 7, 17, 1), (40, 34, 33, 4),
-                                          (20, 4, 16, 2), (22, 5, 16, 2), (26, 70, 12, 2)])
+                                          (20, 4, 16, 2), (22, 5, 16, 2), (26, 70, 12, 2), (24, 12, 40, 3),
+                                          (24, 12, 40, 1)])
 def test_free_running_steps_match(nx, nzs, nyw, P):
     """Grids with 4 span rows or fewer sweep with a row lag of a whole chunk
     (the Gauss-Seidel wrap row would otherwise share a step with row 1); 5
     rows is the smallest grid with the one-position lag; 70 rows span three
-    32-row blocks."""
+    32-row blocks.  The sweeps' plane groups of a slab column run as one
+    thread-block cluster when they are 2..8: 40 planes in 3 slabs (13, 13 and
+    12 planes: 4 plane groups, the last slab's top CTA idle) take that path,
+    40 planes in one slab (10 plane groups) the cooperative launch with
+    global flags."""
     o, g, _ = pair(nx, nzs, nyw, P)
     for s in range(7):
         so, _ = o.step(1, check=False)
