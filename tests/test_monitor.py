@@ -134,3 +134,25 @@ def test_monitor_schedule_over_an_oracle_run(tmp_path):
     assert (tmp_path / "boundarylthickness.dat").read_text() == ref.bl_thickness_text(
         recs[9]["time"], mesh.x1, s["bltkns"], stats["deltastar"], stats["theta"], stats["ht"], stats["reth"])
     r.close()
+
+
+def test_monitor_follows_the_variant_window_and_recycling_start(tmp_path):
+    """originalTBL closes its wall-shear window every 1000 steps (not 500)
+    and its fluctuation energy starts after its recycling start (1000)."""
+    from oracle.bind import OracleRunner
+    wl = small_workload(nx=24, nz_span=12, ny_wall=20)
+    mesh, rp, st = make_state(wl, nproc=2)
+    rp.use_variant(1)
+    st = dict(st, nstep=998, time=0.0998, cont=0, cnt2=0)  # steps 999..1001: 1000 closes the window
+    r = OracleRunner(mesh, rp)
+    r.upload(st)
+    mon = monitor.Monitor(r, tmp_path)
+    assert mon.window == 1000
+    status, recs = mon.step(3)
+    assert status == abi.TBL_OK and [q["nstep"] for q in recs] == [999, 1000, 1001]
+    tw = _numbers(tmp_path / "numrcltauwall.xy")
+    assert len(tw) == 4 * (mesh.nx - 2) and tw[0] == pytest.approx(recs[1]["time"], abs=1e-7)
+    ke = _numbers(tmp_path / "kineticenergy.dat")
+    assert len(ke) == 2 and ke[0] == pytest.approx(recs[2]["time"], rel=1e-9)  # nstep 1001 > 1000 only
+    assert len((tmp_path / "massflow.xy").read_text().splitlines()) == 3
+    r.close()
